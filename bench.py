@@ -1,0 +1,389 @@
+"""Benchmark of the radiosity hot path on GB300.
+
+Default workload: the direct-light pass of a bake (4,096 box faces, 1.33M
+luxels x 4 supersamples, 64 point + 8 spot lights + a 162-direction sky,
+8,208-triangle room whose ceiling is sky).  A step is one full gather; the
+metric is shadow rays traced per second (Mrays/s).  `--workload anyhit` runs
+the 2^20-line occlusion-mask case (12,300 triangles) instead.
+
+Prints ONE JSON line on rank 0.  `--impl reference` times the reference's
+CPU path instead: the C restatement of it under oracle/ (the Go reference has
+no toolchain here), with every host thread, on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SEED = 0
+CPU_SAMPLE_FACES = 1024  # bounded CPU baseline sample: faces [0, 1024) of 4,096
+REF_FACES_PER_STEP = 256  # reference arm: faces per timed step
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _ncu_traffic(kernel_file: str):
+    """DRAM bytes per launch from a committed ncu summary, if present."""
+    p = ROOT / "profiles" / kernel_file
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_full:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.proc = None
+        self.path = None
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _cpu_baseline(lit, faces, threads):
+    from oracle import pyoracle
+
+    s = pyoracle.Scene(lit.xyz, lit.ids)
+    lights = pyoracle.make_lights(lit.lights)
+    t0 = time.perf_counter()
+    _, rays, st = pyoracle.gather_luxels(s, lights, len(lit.lights), lit, 0, faces, ss=4,
+                                         seed=SEED, threads=threads, stats=True)
+    dt = time.perf_counter() - t0
+    return rays, dt, st
+
+
+def run_reference(args, rank):
+    """CPU reference arm: the oracle restatement of the path, every thread."""
+    if rank != 0:
+        return
+    from vrad_gb300 import scenes
+
+    threads = os.cpu_count() or 1
+    lit = scenes.lit_scene(SEED)
+    from oracle import pyoracle
+
+    s = pyoracle.Scene(lit.xyz, lit.ids)
+    lights = pyoracle.make_lights(lit.lights)
+    nf = lit.n_faces
+
+    def step(i):
+        f0 = (i * REF_FACES_PER_STEP) % nf
+        t0 = time.perf_counter()
+        _, rays = pyoracle.gather_luxels(s, lights, len(lit.lights), lit, f0,
+                                         f0 + REF_FACES_PER_STEP, ss=4, seed=SEED, threads=threads)
+        return rays, time.perf_counter() - t0
+
+    for i in range(args.warmup):
+        step(i)
+    tot_r, tot_t = 0, 0.0
+    for i in range(args.steps):
+        r, t = step(args.warmup + i)
+        tot_r += r
+        tot_t += t
+    v = tot_r / tot_t / 1e6
+    sample = (f"{REF_FACES_PER_STEP} of {nf} faces per step (~{tot_r // max(args.steps, 1)} "
+              f"shadow rays), 4 supersamples")
+    line = {
+        "impl": "reference", "metric": "shadow Mrays/s (direct-light gather)", "value": round(v, 3),
+        "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * tot_t / max(args.steps, 1), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "direct light, 4096 faces / 1.33M luxels x 4 samples, 64 point + "
+                               "8 spot + 162-direction sky, 8208 triangles", "sample": sample},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _l2_copy_gbs(torch, dev):
+    """Bandwidth of a torch copy of a 24 MiB buffer that stays in L2."""
+    a = torch.empty(6 << 20, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(200):
+        b.copy_(a)
+    e1.record()
+    torch.cuda.synchronize()
+    return 2 * a.numel() * 4 * 200 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Context, Environment, light_array
+
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+
+        td.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream()
+    lib_ctx = Context(local_rank)
+    lib_ctx.set_stream(stream.cuda_stream)
+    lib = lib_ctx.lib
+
+    if args.workload == "anyhit":
+        sc = scenes.anyhit_scene(SEED)
+        env = Environment(lib_ctx)
+        env.add_triangles(sc.xyz, sc.ids)
+        env.SetupAccelerationStructure()
+        n = sc.starts.shape[0]
+        d_a = torch.from_numpy(sc.starts).to(dev)
+        d_b = torch.from_numpy(sc.stops).to(dev)
+        d_m = torch.empty((n + 31) // 32, dtype=torch.int32, device=dev)
+        units = n
+        kernel = "trace_mask"
+
+        def step_dev():
+            rc = lib.vrg_env_occlusion_mask_d(env.h, d_a.data_ptr(), d_b.data_ptr(), n, -1,
+                                              d_m.data_ptr(), None, None)
+            assert rc == 0, rc
+
+        h_a = torch.from_numpy(sc.starts).pin_memory()
+        h_b = torch.from_numpy(sc.stops).pin_memory()
+        h_m = torch.empty((n + 31) // 32, dtype=torch.int32).pin_memory()
+
+        def step_host():
+            rc = lib.vrg_env_occlusion_mask(env.h, h_a.data_ptr(), h_b.data_ptr(), n, -1,
+                                            h_m.data_ptr(), None, None)
+            assert rc == 0, rc
+
+        h2d, d2h = 24 * n, 4 * ((n + 31) // 32)
+        workload = "any-hit occlusion mask, 2^20 shadow lines, 12,300-triangle box room"
+        bytes_per_unit = None
+    else:
+        lit = scenes.lit_scene(SEED, n_faces=args.faces)
+        env = Environment(lib_ctx)
+        env.add_triangles(lit.xyz, lit.ids)
+        env.SetupAccelerationStructure()
+        env.set_faces(lit)
+        lights = light_array(lit.lights)
+        env.set_lights(lit.lights)
+        nlux = env.num_luxels()
+        d_out = torch.empty((nlux, 3), dtype=torch.float32, device=dev)
+        rays = C.c_uint64()
+        rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(), C.byref(rays))
+        assert rc == 0, rc
+        units = rays.value
+        kernel = "direct_luxels"
+
+        def step_dev():
+            rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(), None)
+            assert rc == 0, rc
+
+        h_out = torch.empty((nlux, 3), dtype=torch.float32).pin_memory()
+        nl = len(lit.lights)
+
+        def step_host():
+            rc = lib.vrg_env_set_lights(env.h, lights, nl)
+            assert rc == 0, rc
+            rc = lib.vrg_env_gather_direct_light(env.h, 4, SEED, h_out.data_ptr(), None)
+            assert rc == 0, rc
+
+        h2d, d2h = 80 * nl, 12 * nlux
+        workload = ("direct light, %d faces / %d luxels x 4 supersamples, 64 point + 8 spot + "
+                    "162-direction sky, %d triangles" % (lit.n_faces, nlux, len(lit.ids)))
+
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    for _ in range(max(args.warmup, 3)):
+        step_dev()
+        flush.zero_()
+    torch.cuda.synchronize()
+
+    lib_ctx.set_timing(True)
+    lib_ctx.reset_stats()
+    launches0 = lib_ctx.launch_count()
+    clocks = Clocks(local_rank) if rank == 0 else None
+    if dist:
+        td.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        evs[k][0].record(stream)
+        step_dev()
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        td.barrier()
+    clk = clocks.stop() if clocks else None
+    launches = lib_ctx.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(step_ms)
+    kms, kn = lib_ctx.kernel_stats(kernel)
+    lib_ctx.set_timing(False)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = units * args.steps * world / (total_ms * 1e-3) / 1e6
+
+    # end to end through the host-buffer C ABI (pinned host memory)
+    for _ in range(2):
+        step_host()
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step_host()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_value = units * world / statistics.mean(e2e_t) / 1e6
+
+    if rank != 0:
+        if dist:
+            td.destroy_process_group()
+        return
+
+    peak, peak_kind = _peaks()
+    threads = os.cpu_count() or 1
+    cpu = None
+    roof = None
+    avg_ms = kms / max(kn, 1)
+    if args.workload == "anyhit":
+        from oracle import pyoracle
+
+        s = pyoracle.Scene(sc.xyz, sc.ids)
+        t0 = time.perf_counter()
+        m, st = pyoracle.Scene.occlusion_mask(s, sc.starts, sc.stops, threads=threads, stats=True)
+        dt = time.perf_counter() - t0
+        nodes, tris = st[:, 0].mean(), st[:, 1].mean()
+        bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
+        cpu = {"value": round(n / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+               "kind": "port", "sample": f"all {n} lines"}
+    else:
+        cpu_faces = min(CPU_SAMPLE_FACES, lit.n_faces)
+        rays_cpu, dt, st = _cpu_baseline(lit, cpu_faces, threads)
+        nodes, tris = st[1] / st[0], st[2] / st[0]
+        bytes_per_unit = 8 * nodes + 48 * tris + (80 + 3) / (units / (4 * nlux))
+        cpu = {"value": round(rays_cpu / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+               "kind": "port",
+               "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
+    achieved = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
+    traffic = _ncu_traffic(f"ncu_{kernel}.txt")
+    l2 = _l2_copy_gbs(torch, dev)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "peak_kind": f"{peak_kind} HBM copy",
+            "kernel": kernel, "kernel_ms": round(avg_ms, 4),
+            "bytes_per_ray": round(bytes_per_unit, 2),
+            "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
+            "l2_copy_gbs": round(l2, 1), "l2_frac": round(achieved / l2, 4)}
+    line = {
+        "metric": "shadow Mrays/s (direct-light gather)" if args.workload != "anyhit"
+        else "shadow Mrays/s (any-hit occlusion mask)",
+        "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 box rooms)",
+        "config": {"workload": workload, "rays_per_step": units,
+                   "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        td.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="direct", choices=["direct", "anyhit"])
+    ap.add_argument("--faces", type=int, default=4096,
+                    help="lit faces of the direct-light scene (smaller only for profiling)")
+    args = ap.parse_args()
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local_rank = _env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

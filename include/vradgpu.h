@@ -1,0 +1,248 @@
+/*
+ * vradgpu.h -- C ABI of the GB300 (sm_103a) radiosity hot path.
+ *
+ * One shared library (libvradgpu.so) stands behind the reference's Go entry
+ * points for the ray tracer, direct-light gathering, transfer building and
+ * the bounce loop.  Plain pointers and sizes only; every call returns an int
+ * status (VRG_OK = 0, negative on error) and the message of the most recent
+ * failure on a context is available from vrg_last_error().
+ *
+ * Ownership: host buffers belong to the caller and are only borrowed for the
+ * duration of the call.  Device memory is owned by the handle that created
+ * it.  Functions ending in _d take device pointers; all others take host
+ * pointers and copy through pinned staging inside the call.
+ *
+ * Threading: a context may be shared by several host threads; each
+ * environment serialises its own calls with a mutex.
+ *
+ * Reference citations are paths inside the reference project.
+ */
+#ifndef VRADGPU_H
+#define VRADGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VRG_OK 0
+#define VRG_ERR_INVALID (-1)     /* bad argument */
+#define VRG_ERR_NOMEM (-2)       /* host or device allocation failed */
+#define VRG_ERR_CUDA (-3)        /* CUDA runtime error */
+#define VRG_ERR_TIMEOUT (-4)     /* a bounded device wait ran out */
+#define VRG_ERR_STATE (-5)       /* call out of order (e.g. trace before build) */
+#define VRG_ERR_UNSUPPORTED (-6) /* feature or size outside the build's limits */
+
+/* raytracer/constants.go:9-11 */
+#define VRG_TRACE_ID_SKY 0x01000000
+#define VRG_TRACE_ID_OPAQUE 0x02000000
+#define VRG_TRACE_ID_STATICPROP 0x04000000
+/* raytracer/constants.go:5-7 */
+#define VRG_RTE_FLAGS_FAST_TREE_GENERATION 1
+#define VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_COLORS 2
+#define VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_MATERIALS 4
+
+/* Source's emittype order, as galaco/bsp worldlight EMIT_* uses it. */
+#define VRG_EMIT_SURFACE 0
+#define VRG_EMIT_POINT 1
+#define VRG_EMIT_SPOTLIGHT 2
+#define VRG_EMIT_SKYLIGHT 3
+#define VRG_EMIT_QUAKELIGHT 4
+#define VRG_EMIT_SKYAMBIENT 5
+
+typedef struct vrg_ctx vrg_ctx;
+typedef struct vrg_env vrg_env;
+
+/* The light fields the gather reads: DirectLight + WorldLight
+ * (common/types/light.go:10-44).  20 x 4 bytes. */
+typedef struct vrg_light {
+    int32_t type;
+    float origin[3];
+    float intensity[3];
+    float normal[3];
+    float stopdot, stopdot2, exponent;
+    float constant_attn, linear_attn, quadratic_attn;
+    float radius;
+    float start_fade, end_fade, cap_distance;
+} vrg_light;
+
+/* Entity keys that rad/lightmap/lights.go:210-341 reads. */
+typedef struct vrg_light_keys {
+    float fifty_percent_distance, zero_percent_distance;
+    int32_t hard_falloff;
+    float constant_attn, linear_attn, quadratic_attn, distance;
+    float inner_cone, cone, exponent;
+} vrg_light_keys;
+
+/* ------------------------------------------------------------------ */
+/* context                                                              */
+/* ------------------------------------------------------------------ */
+
+/* Creates a context on CUDA device `device` with its own non-blocking stream.
+ * device < 0 creates a host-only context: the host algorithms (kd-tree build,
+ * intersection records, light parameters, patch subdivision) work, every
+ * device call returns VRG_ERR_STATE.
+ * (no reference counterpart: the reference is one process with globals) */
+int vrg_ctx_create(int device, vrg_ctx **out);
+void vrg_ctx_destroy(vrg_ctx *ctx);
+/* Message of the last failure on this context ("" if none). */
+const char *vrg_last_error(const vrg_ctx *ctx);
+/* Launch on `stream` (a cudaStream_t) instead of the context's own stream;
+ * NULL restores the context stream. */
+int vrg_ctx_set_stream(vrg_ctx *ctx, void *stream);
+int vrg_ctx_synchronize(vrg_ctx *ctx);
+/* Per-kernel CUDA-event timing of every launch (off by default). */
+int vrg_ctx_set_timing(vrg_ctx *ctx, int enable);
+/* Accumulated device time and launch count of kernel `name` since the last
+ * reset; names: "trace_mask", "trace_closest", "direct_luxels",
+ * "direct_points", "transfer_rows", "transfer_gather", "bounce_spmv",
+ * "bounce_reduce", "batch_queue". */
+int vrg_ctx_kernel_stats(vrg_ctx *ctx, const char *name, double *total_ms, int64_t *launches);
+int vrg_ctx_reset_stats(vrg_ctx *ctx);
+/* Kernels launched by this context since creation (all names). */
+int64_t vrg_ctx_launch_count(const vrg_ctx *ctx);
+
+/* ------------------------------------------------------------------ */
+/* Environment: raytracer/environment.go                                */
+/* ------------------------------------------------------------------ */
+
+/* NewEnvironment (environment.go:434-442) */
+int vrg_env_create(vrg_ctx *ctx, vrg_env **out);
+void vrg_env_destroy(vrg_env *env);
+/* AddTriangleWithMaterial (environment.go:45-69); colour may be NULL. */
+int vrg_env_add_triangle(vrg_env *env, int32_t id, const float *v1, const float *v2,
+                         const float *v3, const float *colour, uint16_t flags, int32_t material);
+/* AddQuad (environment.go:71-75): (v1,v2,v3) id, (v1,v3,v4) id+1 */
+int vrg_env_add_quad(vrg_env *env, int32_t id, const float *v1, const float *v2, const float *v3,
+                     const float *v4, const float *colour);
+/* AddAxisAlignedRectangularSolid (environment.go:77-117) */
+int vrg_env_add_axis_aligned_rectangular_solid(vrg_env *env, int32_t id, const float *mins,
+                                               const float *maxs, const float *colour);
+/* Bulk AddTriangle for n triangles (xyz: 9 floats each), the loop of
+ * cmd/tasks/loadbsp/main.go:276,338. */
+int vrg_env_add_triangles(vrg_env *env, const float *xyz, const int32_t *ids, int64_t n);
+/* SetupAccelerationStructure (environment.go:119-138): SAH kd tree built on
+ * the host with the reference's candidates, costs and partition order, then
+ * the tree and intersection records are uploaded and stay resident. */
+int vrg_env_setup_acceleration_structure(vrg_env *env);
+int64_t vrg_env_num_triangles(const vrg_env *env);
+/* Size of the built tree: nodes, triangle-index-list length, tree height. */
+int vrg_env_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height);
+/* OptimizedKDTree (children word, split float) and TriangleIndexList. */
+int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs);
+/* GetTriangle (environment.go:422-424): the 48-byte TriIntersectData
+ * (raytracer/cache/triangle/triintersectdata.go:3-22) of triangle `index`. */
+int vrg_env_get_triangle(const vrg_env *env, int64_t index, void *out48);
+int vrg_env_bounds(const vrg_env *env, float *mins, float *maxs);
+
+/* Trace4Rays (environment.go:140-145; FourRays raytracer/types/fourrays.go:8-11,
+ * RayTracingResult raytracer/types/result.go:8-12).  origin/direction are
+ * FourVectors in x x x x y y y y z z z z order; hit_ids[i] = triangle index or
+ * -1; surface_normal (may be NULL) in the same SoA order. */
+int vrg_env_trace4_rays(vrg_env *env, const float *origin, const float *direction,
+                        const float *tmin, const float *tmax, int32_t skip_id, int32_t *hit_ids,
+                        float *hit_distance, float *surface_normal);
+/* Closest hit of n rays (origin/direction 3 floats each, AoS); the batched
+ * form of Trace4Rays. */
+int vrg_env_trace_closest(vrg_env *env, const float *origin, const float *direction,
+                          const float *tmin, const float *tmax, int64_t n, int32_t skip_id,
+                          int32_t *out_hit, float *out_t);
+int vrg_env_trace_closest_d(vrg_env *env, const float *origin, const float *direction,
+                            const float *tmin, const float *tmax, int64_t n, int32_t skip_id,
+                            int32_t *out_hit, float *out_t);
+/* TestLineDoesHitSky (raytracer/trace/testline.go:18-94) for n lines:
+ * fraction_visible[i] is 1 or 0; the skip id is TRACE_ID_STATICPROP |
+ * static_prop_to_skip as at testline.go:36. */
+int vrg_env_test_line_does_hit_sky(vrg_env *env, const float *start, const float *stop,
+                                   int64_t n, int32_t static_prop_to_skip,
+                                   float *fraction_visible);
+/* Shadow lines as a 1-bit mask (bit i%32 of word i/32 set = occluded), with
+ * the same semantics; out_hit/out_t (may be NULL) add the closest hit of the
+ * normalised segment. */
+int vrg_env_occlusion_mask(vrg_env *env, const float *start, const float *stop, int64_t n,
+                           int32_t skip_id, uint32_t *out_mask, int32_t *out_hit, float *out_t);
+int vrg_env_occlusion_mask_d(vrg_env *env, const float *start, const float *stop, int64_t n,
+                             int32_t skip_id, uint32_t *out_mask, int32_t *out_hit, float *out_t);
+/* Ray stream (AddToRayStream / FlushStreamEntry / FinishRayStream,
+ * environment.go:162-175): lines are queued on the host, traced in large
+ * batches, and their fraction_visible values are returned in queue order. */
+int vrg_env_add_to_ray_stream(vrg_env *env, const float *start, const float *stop,
+                              int32_t skip_id);
+int vrg_env_flush_stream_entry(vrg_env *env);
+int vrg_env_finish_ray_stream(vrg_env *env, float *fraction_visible, int64_t capacity,
+                              int64_t *count);
+
+/* ------------------------------------------------------------------ */
+/* Lights: rad/lightmap/lights.go                                       */
+/* ------------------------------------------------------------------ */
+
+/* SetLightFalloffParams (lights.go:259-341) */
+int vrg_light_set_falloff_params(const vrg_light_keys *keys, vrg_light *light);
+/* ParseLightSpot (lights.go:210-257) without the entity parse: origin,
+ * intensity and normal are set by the caller. */
+int vrg_light_parse_spot(const vrg_light_keys *keys, vrg_light *light);
+/* ParseLightPoint (lights.go:417-426) */
+int vrg_light_parse_point(const vrg_light_keys *keys, vrg_light *light);
+/* The active light list CreateDirectLights (lights.go:38-116) produces,
+ * copied to the device. */
+int vrg_env_set_lights(vrg_env *env, const vrg_light *lights, int32_t n);
+
+/* ------------------------------------------------------------------ */
+/* Faces, luxels and the direct-light gather                            */
+/* ------------------------------------------------------------------ */
+
+/* Lightmapped faces: axis-aligned rectangles corner + s*u + t*v with unit
+ * normal, nu x nv luxels (the extents CalcFaceExtents computes,
+ * rad/world/face.go:14-90), luxscale = luxels per world unit,
+ * reflectivity/baselight RGB (BaseLightForFace, rad/patches/face.go:210-231;
+ * reflectivity is clamped to 0.99).  tri_face (ntris entries) maps each
+ * triangle to its face or -1.  NULL reflectivity/baselight mean 0. */
+int vrg_env_set_faces(vrg_env *env, int32_t nfaces, const float *corner, const float *u,
+                      const float *v, const float *normal, const int32_t *nu, const int32_t *nv,
+                      const float *luxscale, const float *reflectivity, const float *baselight,
+                      const int32_t *tri_face);
+int64_t vrg_env_num_luxels(const vrg_env *env);
+/* Direct light of every luxel (RGB, luxel order = face order, row-major
+ * nu x nv), averaged over `supersamples` (1 or 4) seeded samples. */
+int vrg_env_gather_direct_light(vrg_env *env, int32_t supersamples, uint64_t seed,
+                                float *out_rgb, uint64_t *out_shadow_rays);
+int vrg_env_gather_direct_light_d(vrg_env *env, int32_t supersamples, uint64_t seed,
+                                  float *out_rgb, uint64_t *out_shadow_rays);
+/* Direct light at n explicit points with normals. */
+int vrg_env_gather_points(vrg_env *env, const float *points, const float *normals, int64_t n,
+                          float *out_rgb, uint64_t *out_shadow_rays);
+
+/* ------------------------------------------------------------------ */
+/* Patches, transfers, bounce: rad/patches, common/types/patch.go       */
+/* ------------------------------------------------------------------ */
+
+/* MakePatches + SubdividePatches (rad/patches/build.go:21-68,
+ * subdivide.go:25-251) for the faces set above. */
+int vrg_env_make_patches(vrg_env *env, float max_chop, float min_chop, int64_t *num_patches,
+                         int64_t *num_leaves);
+/* All patches (parents included); any pointer may be NULL. */
+int vrg_env_get_patches(const vrg_env *env, float *mins, float *maxs, float *center, float *area,
+                        int32_t *face, int32_t *parent, int32_t *child1, int32_t *child2,
+                        int32_t *split_axis, float *split_dist, int32_t *leaf_index);
+/* Transfer lists (Patch.NumTransfers/Transfers, common/types/patch.go:60-61,
+ * Transfer common/types/transfer.go:3-6) of every leaf patch, from k
+ * closest-hit rays along dirs_local (k x 3, local frame: tangent, bitangent,
+ * normal).  Built on the device into CSR and kept resident. */
+int vrg_env_make_transfers(vrg_env *env, const float *dirs_local, int32_t k, int64_t *out_nnz);
+/* CSR copy-out: row_ptr[leaves+1], col[nnz], weight[nnz] (= hits / k). */
+int vrg_env_get_transfers(const vrg_env *env, int64_t *row_ptr, int32_t *col, float *weight);
+/* Direct light at every leaf patch (one sample at centre + 0.125 * normal). */
+int vrg_env_gather_patch_direct(vrg_env *env, float *out_rgb);
+/* Bounce loop: emit = refl * direct + baselight; per bounce add = T emit,
+ * total += add, emit = refl * add; stop after the bounce whose energy delta
+ * sum|add| / sum|total| < rel_tol, or after max_bounces.  out_total (leaves x
+ * 3, may be NULL) is the bounced light (TotalLight, patch.go:33). */
+int vrg_env_bounce_light(vrg_env *env, int32_t max_bounces, float rel_tol, float *out_total,
+                         int32_t *out_bounces, float *out_delta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

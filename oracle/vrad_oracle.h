@@ -1,0 +1,168 @@
+/*
+ * vrad_oracle.h -- CPU oracle for the VRAD radiosity hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
+ * algorithm, used by tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg as the checker.  The product library never links, loads or
+ * calls it.
+ *
+ * Reference files restated (paths inside the reference project):
+ *   raytracer/environment.go:41-138,181-403   triangle soup, SAH kd builder
+ *   raytracer/cache/optimisedtriangle.go:14-103  intersection format, classify
+ *   raytracer/cache/optimisedkdnode.go:8-54    packed node
+ *   raytracer/kdtree/constants.go:25-28        SAH constants
+ *   vmath/polygon/edge.go:5-24, surface.go:5-8 edge equations, box area
+ *   raytracer/trace/testline.go:18-94          shadow-line semantics
+ *   rad/lightmap/lights.go:23,210-341          light falloff parameters
+ *   vmath/quadratic/solver.go:4-63             inverse quadratic solve
+ *   rad/patches/subdivide.go:166-411           patch subdivision
+ *   common/types/patch.go, transfer.go         patch / transfer layout
+ * Gather, transfer building and the bounce loop are absent from the
+ * reference; their semantics are the project's own and are written out in
+ * the comments of vrad_oracle.c beside each function.
+ *
+ * Parity status: unpinned against the reference itself (it has no Go
+ * toolchain here and no golden vectors for this path); pinned by the
+ * known-answer tests in tests/test_oracle_kat.py.
+ */
+#ifndef VRAD_ORACLE_H
+#define VRAD_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_TRACE_ID_SKY        0x01000000
+#define ORC_TRACE_ID_OPAQUE     0x02000000
+#define ORC_TRACE_ID_STATICPROP 0x04000000
+
+#define ORC_MODE_FIXED   0
+#define ORC_MODE_LITERAL 1
+
+/* TriIntersectData (raytracer/cache/triangle/triintersectdata.go:3-22), 48 B. */
+typedef struct {
+    float nx, ny, nz, d;
+    int32_t id;
+    float e[6];
+    uint8_t cs0, cs1, flags, unused;
+} orc_tri;
+
+/* The parts of DirectLight / WorldLight (common/types/light.go:10-44) that
+ * the gather reads.  type uses Source's emittype order:
+ * 0 surface, 1 point, 2 spotlight, 3 skylight, 4 quakelight, 5 skyambient. */
+typedef struct {
+    int32_t type;
+    float origin[3];
+    float intensity[3];
+    float normal[3];
+    float stopdot, stopdot2, exponent;
+    float constant_attn, linear_attn, quadratic_attn;
+    float radius;
+    float start_fade, end_fade, cap_distance;
+} orc_light;
+
+/* Entity key/values that SetLightFalloffParams / ParseLightSpot read. */
+typedef struct {
+    float fifty_percent_distance, zero_percent_distance;
+    int32_t hard_falloff;
+    float constant_attn, linear_attn, quadratic_attn, distance;
+    float inner_cone, cone, exponent;
+} orc_light_keys;
+
+typedef struct orc_scene orc_scene;
+
+/* ---- scene / kd tree ---- */
+orc_scene *orc_scene_new(const float *xyz, const int32_t *ids, const uint8_t *flags,
+                         int64_t ntris, int mode);
+void orc_scene_free(orc_scene *s);
+int64_t orc_scene_num_nodes(const orc_scene *s);
+int64_t orc_scene_num_refs(const orc_scene *s);
+void orc_scene_get_tree(const orc_scene *s, uint32_t *children, float *split, int32_t *refs);
+void orc_scene_get_tris(const orc_scene *s, orc_tri *out);
+void orc_scene_bounds(const orc_scene *s, float *bmin, float *bmax);
+int orc_scene_depth(const orc_scene *s);
+
+/* intersection format of one triangle (fixed semantics) */
+void orc_tri_format(const float *xyz9, int32_t id, uint8_t flags, orc_tri *out);
+/* GetEdgeEquation (vmath/polygon/edge.go:5-24); p1,p2,inside are xyz */
+void orc_edge_equation(const float *p1, const float *p2, int c1, int c2, const float *inside,
+                       float *out3);
+
+/* ---- trace ---- */
+/* closest hit: out_hit = triangle index (insertion order) or -1; out_t = t.
+ * brute != 0 tests every triangle instead of walking the tree.
+ * stats (optional, 3 x n): nodes visited, triangles tested, leaves visited. */
+void orc_trace_closest(const orc_scene *s, const float *orig, const float *dir,
+                       const float *tmin, const float *tmax, int64_t n, int32_t skip_id,
+                       int brute, int threads, int32_t *out_hit, float *out_t, uint32_t *stats);
+void orc_trace_any(const orc_scene *s, const float *orig, const float *dir,
+                   const float *tmin, const float *tmax, int64_t n, int32_t skip_id,
+                   int brute, int threads, uint8_t *out_hit, uint32_t *stats);
+/* TestLineDoesHitSky semantics per line; frac = fractionVisible (0 or 1). */
+void orc_test_lines(const orc_scene *s, const float *start, const float *stop, int64_t n,
+                    int32_t skip_id, int brute, int threads, float *out_frac);
+/* 1-bit occlusion mask (bit i of word i/32 set = occluded) and, if out_hit is
+ * non-null, the closest-hit triangle index and t of the normalised segment. */
+void orc_occlusion_mask(const orc_scene *s, const float *start, const float *stop, int64_t n,
+                        int32_t skip_id, int threads, uint32_t *out_mask,
+                        int32_t *out_hit, float *out_t, uint32_t *stats);
+
+/* ---- lights ---- */
+int orc_solve_inverse_quadratic(float x1, float y1, float x2, float y2, float x3, float y3,
+                                float *a, float *b, float *c);
+int orc_solve_inverse_quadratic_monotonic(float x1, float y1, float x2, float y2, float x3,
+                                          float y3, float *a, float *b, float *c);
+void orc_set_light_falloff(const orc_light_keys *k, orc_light *l);
+void orc_parse_light_spot(const orc_light_keys *k, orc_light *l);
+
+/* ---- direct light ---- */
+/* Gather at explicit points (one sample each). rays_out counts shadow rays. */
+void orc_gather_points(const orc_scene *s, const orc_light *lights, int nlights,
+                       const float *pts, const float *nrm, int64_t n, int threads,
+                       float *out_rgb, uint64_t *rays_out);
+/* Luxel supersample gather.  faces: corner,u,v,normal (3 floats each), nu,nv.
+ * luxel_offset[f] = first luxel of face f.  Writes RGB per luxel. */
+void orc_gather_luxels(const orc_scene *s, const orc_light *lights, int nlights,
+                       const float *corner, const float *u, const float *v, const float *nrm,
+                       const int32_t *nu, const int32_t *nv, const int64_t *luxel_offset,
+                       int32_t face_begin, int32_t face_end, int supersamples, uint64_t seed,
+                       int threads, float *out_rgb, uint64_t *rays_out, uint64_t *stats_out);
+/* the sample points the luxel gather uses (for cross-checks) */
+void orc_luxel_samples(const float *corner, const float *u, const float *v, const float *nrm,
+                       const int32_t *nu, const int32_t *nv, const int64_t *luxel_offset,
+                       int32_t face, int supersamples, uint64_t seed, float *out_pts);
+
+/* ---- patches ---- */
+/* Subdivide axis-aligned rectangular faces.  Returns the number of patches
+ * (parents included) and fills the arrays when they are non-null (call once
+ * with nulls to size).  leaf_index[p] = dense leaf number or -1. */
+int64_t orc_make_patches(const float *corner, const float *u, const float *v, const float *nrm,
+                         const float *luxscale, int32_t nfaces, float max_chop, float min_chop,
+                         float *mins, float *maxs, float *center, float *area, int32_t *face,
+                         int32_t *parent, int32_t *child1, int32_t *child2, int32_t *split_axis,
+                         float *split_dist, int32_t *leaf_index);
+
+/* ---- transfers ---- */
+/* Per leaf patch, K rays along dirs_local (lx,ly,lz) in the frame (T1,T2,N);
+ * counts closest hits per target leaf patch.  Rows are written into the
+ * caller's buffers: row_ptr[P+1] (int64), col/cnt arrays of capacity cap.
+ * Returns total nnz (or -1 if cap is too small; row_ptr is still filled). */
+int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t npatches_all,
+                           const float *mins, const float *maxs, const float *center,
+                           const int32_t *face, const int32_t *child1, const int32_t *child2,
+                           const int32_t *split_axis, const float *split_dist,
+                           const int32_t *leaf_index, const int32_t *face_root,
+                           const float *fnormal, const float *fu,
+                           const float *dirs_local, int32_t k, int threads,
+                           int64_t *row_ptr, int32_t *col, int32_t *cnt, int64_t cap);
+
+/* ---- bounce (float64) ---- */
+int orc_bounce_f64(int64_t nrows, const int64_t *row_ptr, const int32_t *col, const float *w,
+                   const float *refl, const float *direct, const float *base, int max_bounces,
+                   double tol, double *out_total, double *out_deltas);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,161 @@
+"""GPU parity of the trace kernels through the C ABI: 1-bit occlusion masks,
+closest-hit triangle ids and distances bit-exact against the oracle."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env0(gpu_ctx, anyhit_scene):
+    from vrad_gb300.environment import Environment
+
+    env = Environment(gpu_ctx)
+    env.add_triangles(anyhit_scene.xyz, anyhit_scene.ids)
+    env.SetupAccelerationStructure()
+    return env
+
+
+@pytest.fixture(scope="module")
+def oscene0(oracle, anyhit_scene):
+    return oracle.Scene(anyhit_scene.xyz, anyhit_scene.ids)
+
+
+def test_occlusion_mask_full_config(env0, oscene0, anyhit_scene):
+    # 2^20 shadow lines, 12,300 triangles: every mask bit equal
+    sc = anyhit_scene
+    mask = env0.occlusion_mask(sc.starts, sc.stops)
+    ref = oscene0.occlusion_mask(sc.starts, sc.stops, threads=16)
+    assert mask.shape == ref.shape
+    diff = int(np.unpackbits((mask ^ ref).view(np.uint8)).sum())
+    assert diff == 0, f"{diff} mask bits differ"
+    occ = np.unpackbits(mask.view(np.uint8), bitorder="little")[: len(sc.starts)]
+    assert 0.05 < occ.mean() < 0.95
+
+
+def test_closest_hit_full_config(env0, oscene0, anyhit_scene):
+    sc = anyhit_scene
+    mask, hit, t = env0.occlusion_mask(sc.starts, sc.stops, closest=True)
+    rmask, rhit, rt = oscene0.occlusion_mask(sc.starts, sc.stops, threads=16, closest=True)
+    assert np.array_equal(mask, rmask)
+    assert np.array_equal(hit, rhit)
+    assert bits_equal(t, rt)
+
+
+def test_closest_hit_equals_brute_force(env0, oscene0, anyhit_scene):
+    sc = anyhit_scene
+    n = 16384
+    d = (sc.stops[:n] - sc.starts[:n]).astype(np.float32)
+    ln = np.sqrt((d * d).sum(1)).astype(np.float32)
+    dirs = (d / ln[:, None]).astype(np.float32)
+    hit, t = env0.trace_closest(sc.starts[:n], dirs, 0.0, ln)
+    bh, bt = oscene0.trace_closest(sc.starts[:n], dirs, 0.0, ln, brute=True, threads=16)
+    assert np.array_equal(hit, bh) and bits_equal(t, bt)
+
+
+def test_long_and_axis_parallel_rays(env0, oscene0):
+    rng = np.random.default_rng(11)
+    n = 20000
+    o = rng.uniform(1, 4095, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 4, 0] = 0.0  # parallel to x splits
+    d[n // 4: n // 2, 1:] = 0.0  # along x only
+    d[n // 2: n // 2 + 100] = 0.0  # zero direction: never hits
+    ln = np.sqrt((d * d).sum(1)).astype(np.float32)
+    ok = ln > 0
+    d[ok] = d[ok] / ln[ok, None]
+    tmax = np.full(n, 60000.0, np.float32)
+    hit, t = env0.trace_closest(o, d, 0.0, tmax)
+    rh, rt = oscene0.trace_closest(o, d, 0.0, tmax, threads=16)
+    assert np.array_equal(hit, rh) and bits_equal(t, rt)
+    bh, _ = oscene0.trace_closest(o[:4000], d[:4000], 0.0, tmax[:4000], brute=True, threads=16)
+    assert np.array_equal(hit[:4000], bh)
+
+
+def test_trace4rays_soa(env0, oscene0, anyhit_scene):
+    sc = anyhit_scene
+    a, b = sc.starts[:4], sc.stops[:4]
+    d = (b - a).astype(np.float32)
+    ln = np.sqrt((d * d).sum(1)).astype(np.float32)
+    d = (d / ln[:, None]).astype(np.float32)
+    hit, dist, nrm = env0.Trace4Rays(a.T.copy(), d.T.copy(), np.zeros(4, np.float32), ln)
+    rh, rt = oscene0.trace_closest(a, d, 0.0, ln)
+    assert hit.tolist() == rh.tolist() and bits_equal(dist, rt)
+
+
+def test_test_line_does_hit_sky_with_sky_ceiling(gpu_ctx, oracle, lit_scene):
+    # room ceiling tagged TRACE_ID_SKY: lines ending above it count as visible
+    from vrad_gb300.environment import Environment
+
+    env = Environment(gpu_ctx)
+    env.add_triangles(lit_scene.xyz, lit_scene.ids)
+    env.SetupAccelerationStructure()
+    rng = np.random.default_rng(2)
+    n = 200000
+    a = rng.uniform(1, 4095, (n, 3)).astype(np.float32)
+    b = rng.uniform(1, 4095, (n, 3)).astype(np.float32)
+    b[: n // 2, 2] = 60000.0  # through the ceiling
+    frac = env.test_line_does_hit_sky(a, b)
+    s = oracle.Scene(lit_scene.xyz, lit_scene.ids)
+    ref = s.test_lines(a, b, skip=-1, threads=16)
+    assert np.array_equal(frac, ref)
+    assert 0.0 < frac[: n // 2].mean() < 1.0
+    # ray stream API gives the same answers in queue order
+    for i in range(64):
+        env.AddToRayStream(a[i], b[i], -1)
+    env.FlushStreamEntry()
+    assert np.array_equal(env.FinishRayStream(64), ref[:64])
+
+
+def test_skip_id_and_zero_length(gpu_ctx, oracle):
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    soup = scenes.TriangleSoup()
+    soup.add_box(0x04000000 | 7, (10, 10, 10), (20, 20, 20))  # a "static prop"
+    soup.add_box(0x02000000, (40, 10, 10), (50, 20, 20))
+    xyz, ids = soup.arrays()
+    env = Environment(gpu_ctx)
+    env.add_triangles(xyz, ids)
+    env.SetupAccelerationStructure()
+    a = np.array([[0, 15.5, 15.25], [0, 15.5, 15.25], [5, 5, 5]], np.float32)
+    b = np.array([[30, 15.5, 15.25], [60, 15.5, 15.25], [5, 5, 5]], np.float32)
+    # testline.go:36 skip id = TRACE_ID_STATICPROP | staticPropToSkip
+    got = env.test_line_does_hit_sky(a, b, static_prop_to_skip=7)
+    assert got.tolist() == [1.0, 0.0, 1.0]
+    got = env.test_line_does_hit_sky(a, b, static_prop_to_skip=-1)
+    assert got.tolist() == [0.0, 0.0, 1.0]
+    s = oracle.Scene(xyz, ids)
+    assert s.test_lines(a, b, skip=0x04000000 | 7).tolist() == [1.0, 0.0, 1.0]
+
+
+def test_empty_scene(gpu_ctx):
+    from vrad_gb300.environment import Environment
+
+    env = Environment(gpu_ctx)
+    env.SetupAccelerationStructure()
+    m = env.occlusion_mask(np.zeros((33, 3), np.float32), np.ones((33, 3), np.float32))
+    assert (m == 0).all()
+    hit, t = env.trace_closest(np.zeros((5, 3)), np.ones((5, 3)), 0.0, 10.0)
+    assert (hit == -1).all()
+
+
+def test_device_entry_point_and_launch_count(env0, oscene0, anyhit_scene, gpu_ctx):
+    import torch
+
+    sc = anyhit_scene
+    n = 1 << 16
+    a = torch.from_numpy(sc.starts[:n]).cuda()
+    b = torch.from_numpy(sc.stops[:n]).cuda()
+    m = torch.zeros((n + 31) // 32, dtype=torch.int32, device="cuda")
+    before = gpu_ctx.launch_count()
+    torch.cuda.synchronize()
+    rc = env0.lib.vrg_env_occlusion_mask_d(env0.h, a.data_ptr(), b.data_ptr(), n, -1,
+                                           m.data_ptr(), None, None)
+    assert rc == 0
+    gpu_ctx.synchronize()
+    assert gpu_ctx.launch_count() == before + 1
+    ref = oscene0.occlusion_mask(sc.starts[:n], sc.stops[:n], threads=16)
+    assert np.array_equal(m.cpu().numpy().view(np.uint32), ref)

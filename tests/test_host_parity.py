@@ -1,0 +1,144 @@
+"""Host algorithms of libvradgpu.so (no GPU: host-only context) against the
+oracle: kd tree, intersection records, light parameters, patch subdivision,
+and the C ABI's exported symbols."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import bits_equal, small_lit_scene
+
+
+def _env(host_ctx, xyz, ids):
+    from vrad_gb300.environment import Environment
+
+    env = Environment(host_ctx)
+    env.add_triangles(xyz, ids)
+    env.SetupAccelerationStructure()
+    return env
+
+
+def test_every_header_symbol_is_exported(vlib):
+    from vrad_gb300 import _lib
+
+    names = _lib.header_symbols()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(vlib, n)]
+    assert not missing, missing
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("which", ["anyhit", "lit", "random"])
+def test_kd_tree_matches_oracle(oracle, host_ctx, which, anyhit_scene, lit_scene):
+    if which == "anyhit":
+        xyz, ids = anyhit_scene.xyz, anyhit_scene.ids
+    elif which == "lit":
+        xyz, ids = lit_scene.xyz, lit_scene.ids
+    else:  # arbitrary (non axis-aligned, overlapping) triangles
+        rng = np.random.default_rng(5)
+        c = rng.uniform(0, 1000, (3000, 1, 3))
+        xyz = (c + rng.normal(0, 30, (3000, 3, 3))).reshape(-1, 9).astype(np.float32)
+        ids = np.full(3000, 0x02000000, np.int32)
+    env = _env(host_ctx, xyz, ids)
+    ch, sp, refs, height = env.tree()
+    s = oracle.Scene(xyz, ids)
+    och, osp, orefs = s.tree()
+    assert np.array_equal(ch, och)
+    assert bits_equal(sp, osp)
+    assert np.array_equal(refs, orefs)
+    assert height < 32
+    assert np.array_equal(env.triangle_records(), s.tri_records())
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 7, 25])
+def test_kd_tree_small_and_degenerate(oracle, host_ctx, n):
+    rng = np.random.default_rng(n)
+    xyz = rng.uniform(0, 10, (n, 9)).astype(np.float32)
+    if n >= 3:
+        xyz[0, 2::3] = 1.0  # a triangle flat in z
+        xyz[1] = xyz[1, :3].tolist() * 3  # a degenerate (point) triangle
+    ids = np.full(n, 0x02000000, np.int32)
+    env = _env(host_ctx, xyz, ids)
+    ch, sp, refs, _ = env.tree()
+    och, osp, orefs = oracle.Scene(xyz, ids).tree()
+    assert np.array_equal(ch, och) and bits_equal(sp, osp) and np.array_equal(refs, orefs)
+
+
+def test_axis_aligned_solid_and_quad_match_soup(host_ctx):
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    env = Environment(host_ctx)
+    env.AddAxisAlignedRectangularSolid(0x02000000, (1, 2, 3), (4, 6, 9))
+    env.AddQuad(0x01000000, (0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0))
+    env.SetupAccelerationStructure()
+    soup = scenes.TriangleSoup()
+    soup.add_box(0x02000000, (1, 2, 3), (4, 6, 9))
+    soup.add_quad(0x01000000, (0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0))
+    xyz, ids = soup.arrays()
+    recs = env.triangle_records()
+    assert env.num_triangles() == 14
+    assert recs[:, 4].view(np.int32).tolist() == ids.tolist()
+
+
+def test_lights_match_oracle(oracle, lit_scene):
+    from vrad_gb300.environment import light_array
+    from vrad_gb300.scenes import Light
+
+    extra = [Light(1, (1, 2, 3), (10, 20, 30), keys=dict(fifty_percent_distance=120.0,
+                                                         zero_percent_distance=500.0)),
+             Light(1, (1, 2, 3), (10, 20, 30), keys=dict(fifty_percent_distance=120.0,
+                                                         zero_percent_distance=500.0,
+                                                         hard_falloff=1)),
+             Light(1, (1, 2, 3), (10, 20, 30), keys=dict(constant_attn=1.0, linear_attn=0.5)),
+             Light(2, (1, 2, 3), (1, 1, 1), (0, 0, -1), keys=dict(inner_cone=120.0, cone=150.0))]
+    lights = lit_scene.lights + extra
+    mine = light_array(lights)
+    ref = oracle.make_lights(lights)
+    n = len(lights)
+    assert bytes(mine)[: 80 * n] == bytes(ref)[: 80 * n]
+
+
+def test_patches_match_oracle(oracle, host_ctx):
+    lit = small_lit_scene(240)
+    env = _env(host_ctx, lit.xyz, lit.ids)
+    env.set_faces(lit)
+    P = env.make_patches()
+    O = oracle.make_patches(lit)
+    for k in ("mins", "maxs", "center", "area", "split_dist"):
+        assert bits_equal(P[k], O[k]), k
+    for k in ("face", "parent", "child1", "child2", "split_axis", "leaf_index"):
+        assert np.array_equal(P[k], O[k]), k
+    assert P["n_leaves"] == int((O["leaf_index"] >= 0).sum())
+    # every leaf spans < 4 luxels (64 units at 16-unit luxels) on each axis
+    leaf = O["leaf_index"] >= 0
+    ext = (O["maxs"] - O["mins"])[leaf] / 16.0
+    assert (ext < 4.0).all()
+
+
+def test_device_calls_refused_on_host_context(host_ctx, anyhit_scene):
+    from vrad_gb300._lib import VrgError
+
+    env = _env(host_ctx, anyhit_scene.xyz[:100], anyhit_scene.ids[:100])
+    with pytest.raises(VrgError, match="call out of order"):
+        env.occlusion_mask(anyhit_scene.starts[:4], anyhit_scene.stops[:4])
+
+
+def test_bad_inputs_are_rejected(host_ctx, vlib):
+    from vrad_gb300._lib import VrgError
+    from vrad_gb300.environment import Environment
+
+    env = Environment(host_ctx)
+    env.AddTriangle(1, (0, 0, 0), (1, 0, 0), (0, 1, 0))
+    # tracing before SetupAccelerationStructure
+    with pytest.raises(VrgError):
+        env.occlusion_mask(np.zeros((1, 3)), np.ones((1, 3)))
+    env.SetupAccelerationStructure()
+    # adding triangles after the build
+    with pytest.raises(VrgError, match="call out of order"):
+        env.AddTriangle(1, (0, 0, 0), (1, 0, 0), (0, 1, 0))
+    # null pointers
+    assert vlib.vrg_env_add_triangle(env.h, 1, None, None, None, None, 0, 0) == -1
+    h = C.c_void_p()
+    assert vlib.vrg_ctx_create(0, None) == -1
+    assert vlib.vrg_env_create(None, C.byref(h)) == -1

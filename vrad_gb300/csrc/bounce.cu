@@ -1,0 +1,230 @@
+// bounce.cu -- the radiosity bounce loop over the CSR transfer lists.  The
+// reference keeps only the state (Patch.TotalLight, DirectLight,
+// Reflectivity, BaseLight: common/types/patch.go:33-42) and the bounce count
+// (numBounce, rad/patches/subdivide.go:19); the loop is the project's own
+// Jacobi gather:
+//   emit = refl * direct + base ; total = 0
+//   per bounce: add_i = sum_j w_ij emit_j ; total += add ; emit = refl * add
+//   delta = sum |add|_1 / sum |total|_1 ; stop after the bounce whose delta
+//   is below the tolerance, or after max_bounces.
+// Each bounce is one SpMV kernel plus one single-block reduction; a CUDA
+// graph holds several bounces and the kernels turn into no-ops once the
+// device-side control block says the loop is done.
+#include <algorithm>
+
+#include "vrg_internal.h"
+
+namespace vrg {
+
+namespace {
+
+constexpr int kSpmvThreads = 256;
+constexpr int kGraphBounces = 8;
+
+struct BounceControl {
+    int32_t done;
+    int32_t iters;
+    int32_t max_iters;
+    float tol;
+    float last_delta;
+    float pad[3];
+};
+
+__global__ void k_bounce_init(const LeafInfo *__restrict__ info, const float *__restrict__ direct,
+                              float4 *__restrict__ emit, float4 *__restrict__ total, int64_t n,
+                              BounceControl *ctl, int32_t max_iters, float tol) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float4 r = info[i].refl, b = info[i].base;
+        emit[i] = make_float4(__fadd_rn(__fmul_rn(r.x, direct[3 * i]), b.x),
+                              __fadd_rn(__fmul_rn(r.y, direct[3 * i + 1]), b.y),
+                              __fadd_rn(__fmul_rn(r.z, direct[3 * i + 2]), b.z), 0.0f);
+        total[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->done = max_iters <= 0;
+        ctl->iters = 0;
+        ctl->max_iters = max_iters;
+        ctl->tol = tol;
+        ctl->last_delta = 0.0f;
+    }
+}
+
+// One warp per row; lanes stride over the row's entries, then a butterfly
+// sum.  Per-block sums of |add| and |total| go to partials[2*block].
+__global__ void __launch_bounds__(kSpmvThreads) k_bounce_spmv(
+    const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
+    const float *__restrict__ w, const float4 *__restrict__ emit_in, float4 *__restrict__ emit_out,
+    float4 *__restrict__ total, const LeafInfo *__restrict__ info, int64_t n,
+    const BounceControl *__restrict__ ctl, double *__restrict__ partials) {
+    if (*(volatile const int32_t *)&ctl->done) return;
+    __shared__ double red[2][kSpmvThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double sa = 0.0, st = 0.0;
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nwarps) {
+        const int64_t b = row_ptr[row], e = row_ptr[row + 1];
+        float ar = 0.0f, ag = 0.0f, ab = 0.0f;
+        int64_t i = b + lane;
+        for (; i + 96 < e; i += 128) {
+            const int32_t c0 = __ldg(col + i), c1 = __ldg(col + i + 32), c2 = __ldg(col + i + 64), c3 = __ldg(col + i + 96);
+            const float w0 = __ldg(w + i), w1 = __ldg(w + i + 32), w2 = __ldg(w + i + 64), w3 = __ldg(w + i + 96);
+            const float4 e0 = __ldg(emit_in + c0), e1 = __ldg(emit_in + c1), e2 = __ldg(emit_in + c2), e3 = __ldg(emit_in + c3);
+            ar += w0 * e0.x + w1 * e1.x + w2 * e2.x + w3 * e3.x;
+            ag += w0 * e0.y + w1 * e1.y + w2 * e2.y + w3 * e3.y;
+            ab += w0 * e0.z + w1 * e1.z + w2 * e2.z + w3 * e3.z;
+        }
+        for (; i < e; i += 32) {
+            const float wv = __ldg(w + i);
+            const float4 ev = __ldg(emit_in + __ldg(col + i));
+            ar += wv * ev.x;
+            ag += wv * ev.y;
+            ab += wv * ev.z;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ar += __shfl_xor_sync(0xffffffffu, ar, o);
+            ag += __shfl_xor_sync(0xffffffffu, ag, o);
+            ab += __shfl_xor_sync(0xffffffffu, ab, o);
+        }
+        if (lane == 0) {
+            float4 t = total[row];
+            t.x += ar;
+            t.y += ag;
+            t.z += ab;
+            total[row] = t;
+            const float4 r = info[row].refl;
+            emit_out[row] = make_float4(r.x * ar, r.y * ag, r.z * ab, 0.0f);
+            sa += (double)fabsf(ar) + (double)fabsf(ag) + (double)fabsf(ab);
+            st += (double)fabsf(t.x) + (double)fabsf(t.y) + (double)fabsf(t.z);
+        }
+    }
+    if (lane == 0) {
+        red[0][wid] = sa;
+        red[1][wid] = st;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, t = 0.0;
+        for (int k = 0; k < kSpmvThreads / 32; k++) {
+            a += red[0][k];
+            t += red[1][k];
+        }
+        partials[2 * blockIdx.x] = a;
+        partials[2 * blockIdx.x + 1] = t;
+    }
+}
+
+// Sums the block partials in a fixed order and advances the control block.
+__global__ void k_bounce_reduce(BounceControl *ctl, const double *__restrict__ partials, int nblocks) {
+    if (*(volatile int32_t *)&ctl->done) return;
+    __shared__ double sa[256], st[256];
+    double a = 0.0, t = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        a += partials[2 * i];
+        t += partials[2 * i + 1];
+    }
+    sa[threadIdx.x] = a;
+    st[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sa[threadIdx.x] += sa[threadIdx.x + o];
+            st[threadIdx.x] += st[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const float delta = st[0] > 0.0 ? (float)(sa[0] / st[0]) : 0.0f;
+        ctl->last_delta = delta;
+        ctl->iters += 1;
+        if (delta < ctl->tol || ctl->iters >= ctl->max_iters) ctl->done = 1;
+    }
+}
+
+}  // namespace
+
+int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounces, float *delta) {
+    vrg_ctx *ctx = env->ctx;
+    const int64_t n = (int64_t)env->patches.leaf_patch.size();
+    VRG_CUDA(ctx, env->d_emit.reserve(2 * 16 * (size_t)std::max<int64_t>(n, 1)));
+    VRG_CUDA(ctx, env->d_total.reserve(16 * (size_t)std::max<int64_t>(n, 1)));
+    const int nblocks = ctx->num_sms * 4;
+    VRG_CUDA(ctx, env->d_partials.reserve(16 * (size_t)nblocks));
+    VRG_CUDA(ctx, env->d_control.reserve(sizeof(BounceControl)));
+    float4 *e0 = env->d_emit.as<float4>(), *e1 = e0 + std::max<int64_t>(n, 1);
+    BounceControl *ctl = env->d_control.as<BounceControl>();
+    const int ib = (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), (int64_t)ctx->num_sms * 8);
+    cudaEvent_t ev = nullptr;
+    timing_begin(ctx, "bounce_init", &ev);
+    k_bounce_init<<<ib, 256, 0, ctx->stream>>>(env->d_leaf_info.as<LeafInfo>(), env->d_leaf_direct.as<float>(), e0,
+                                               env->d_total.as<float4>(), n, ctl, max_bounces, rel_tol);
+    VRG_CUDA(ctx, cudaGetLastError());
+    timing_end(ctx, "bounce_init", ev);
+
+    auto one_bounce = [&](float4 *in, float4 *out) -> cudaError_t {
+        cudaEvent_t ev2 = nullptr;
+        timing_begin(ctx, "bounce_spmv", &ev2);
+        k_bounce_spmv<<<nblocks, kSpmvThreads, 0, ctx->stream>>>(
+            env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), in, out,
+            env->d_total.as<float4>(), env->d_leaf_info.as<LeafInfo>(), n, ctl, env->d_partials.as<double>());
+        cudaError_t e = cudaGetLastError();
+        timing_end(ctx, "bounce_spmv", ev2);
+        if (e != cudaSuccess) return e;
+        timing_begin(ctx, "bounce_reduce", &ev2);
+        k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, env->d_partials.as<double>(), nblocks);
+        e = cudaGetLastError();
+        timing_end(ctx, "bounce_reduce", ev2);
+        return e;
+    };
+
+    BounceControl h{};
+    int32_t launched = 0;
+    // With timing on, bounces launch one by one so each kernel gets events;
+    // otherwise a CUDA graph of kGraphBounces bounces is replayed.
+    if (ctx->timing) {
+        while (launched < max_bounces) {
+            VRG_CUDA(ctx, one_bounce((launched & 1) ? e1 : e0, (launched & 1) ? e0 : e1));
+            launched++;
+            if ((launched % kGraphBounces) == 0 || launched == max_bounces) {
+                VRG_CUDA(ctx, cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+                VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                if (h.done) break;
+            }
+        }
+    } else if (max_bounces > 0) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaStream_t cs = ctx->stream;
+        VRG_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaSuccess;
+        for (int b = 0; b < kGraphBounces && ce == cudaSuccess; b++) ce = one_bounce((b & 1) ? e1 : e0, (b & 1) ? e0 : e1);
+        cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "bounce capture");
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "cudaStreamEndCapture");
+        VRG_CUDA(ctx, cudaGraphInstantiate(&exec, graph, 0));
+        cudaGraphDestroy(graph);
+        while (launched < max_bounces) {
+            cudaError_t le = cudaGraphLaunch(exec, cs);
+            if (le != cudaSuccess) {
+                cudaGraphExecDestroy(exec);
+                return cuda_fail(ctx, le, "cudaGraphLaunch");
+            }
+            launched += kGraphBounces;
+            cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, cs);
+            cudaError_t se = cudaStreamSynchronize(cs);
+            if (se != cudaSuccess) {
+                cudaGraphExecDestroy(exec);
+                return cuda_fail(ctx, se, "bounce graph");
+            }
+            if (h.done) break;
+        }
+        cudaGraphExecDestroy(exec);
+    }
+    VRG_CUDA(ctx, cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *bounces = h.iters;
+    *delta = h.last_delta;
+    return VRG_OK;
+}
+
+}  // namespace vrg

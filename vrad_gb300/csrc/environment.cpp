@@ -1,0 +1,180 @@
+// environment.cpp -- the ray-trace environment (raytracer/environment.go):
+// triangle soup, intersection format, acceleration structure and its
+// upload to the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "vrg_internal.h"
+
+namespace vrg {
+
+// GetEdgeEquation (vmath/polygon/edge.go:5-24): the line through p1,p2 in the
+// (c1,c2) projection, signed and scaled so it equals 1 at `inside`.
+void edge_equation(const float *p1, const float *p2, int c1, int c2, const float *inside,
+                   float *out3) {
+    float nx = p1[c2] - p2[c2];
+    float ny = p2[c1] - p1[c1];
+    float d = -(nx * p1[c1] + ny * p1[c2]);
+    float trial = (inside[c1] * nx + inside[c2] * ny) + d;
+    if (trial < 0) {
+        nx = -nx;
+        ny = -ny;
+        d = -d;
+        trial = -trial;
+    }
+    out3[0] = nx / trial;
+    out3[1] = ny / trial;
+    out3[2] = d / trial;
+}
+
+// ChangeIntoIntersectionFormat (raytracer/cache/optimisedtriangle.go:30-78):
+// N = normalize(e1 x e2) as v * (1/sqrt((x*x + y*y) + z*z)), D = N.p1, drop the
+// axis of largest |N| (first on ties), edge equations of p1p2 (1 at p3) and
+// p2p3 (1 at p1) in the two kept coordinates.
+void tri_intersect_format(const float *xyz9, int32_t id, uint8_t flags, TriRecord *out,
+                          uint32_t tri_index) {
+    (void)flags;
+    const float *p1 = xyz9, *p2 = xyz9 + 3, *p3 = xyz9 + 6;
+    const float e1[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+    const float e2[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
+    float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                  e1[0] * e2[1] - e1[1] * e2[0]};
+    const float len = std::sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2]);
+    const float inv = 1.0f / len;
+    for (float &c : n) c = c * inv;
+    int drop = 0;
+    for (int c = 1; c < 3; c++)
+        if (std::fabs(n[c]) > std::fabs(n[drop])) drop = c;
+    const int cs0 = (drop + 1) % 3, cs1 = (drop + 2) % 3;
+    float ea[3], eb[3];
+    edge_equation(p1, p2, cs0, cs1, p3, ea);
+    edge_equation(p2, p3, cs0, cs1, p1, eb);
+    out->nx = n[0];
+    out->ny = n[1];
+    out->nz = n[2];
+    out->d = (n[0] * p1[0] + n[1] * p1[1]) + n[2] * p1[2];
+    out->e0 = ea[0];
+    out->e1 = ea[1];
+    out->e2 = ea[2];
+    out->e3 = eb[0];
+    out->e4 = eb[1];
+    out->e5 = eb[2];
+    out->id = id;
+    out->idx_drop = (tri_index << 2) | (uint32_t)drop;
+}
+
+}  // namespace vrg
+
+using namespace vrg;
+
+extern "C" {
+
+int vrg_env_setup_acceleration_structure(vrg_env *env) {
+    if (!env) return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(env->mu);
+    vrg_ctx *ctx = env->ctx;
+    const int64_t n = (int64_t)env->ids.size();
+    if (n >= (int64_t)1 << 30) return fail(ctx, VRG_ERR_UNSUPPORTED, "more than 2^30 triangles");
+    build_kd_tree(env->xyz, env->tree, env->min_bound, env->max_bound);
+    if (env->tree.height >= kStackMax)
+        return fail(ctx, VRG_ERR_UNSUPPORTED, "kd tree deeper than the traversal stack");
+
+    env->tri_records.resize(n);
+    SceneGeom &g = env->geom;
+    memset(&g, 0, sizeof g);
+    for (int a = 0; a < 3; a++) {
+        g.bmin[a] = env->min_bound[a];
+        g.bmax[a] = env->max_bound[a];
+        g.smin[a] = INFINITY;
+        g.smax[a] = -INFINITY;
+    }
+    g.ntris = n;
+    float scale = 0.0f;
+    for (int64_t t = 0; t < n; t++) {
+        const float *v = &env->xyz[9 * t];
+        tri_intersect_format(v, env->ids[t], env->flags[t], &env->tri_records[t], (uint32_t)t);
+        for (int k = 0; k < 9; k++) scale = std::max(scale, std::fabs(v[k]));
+        if (env->ids[t] & VRG_TRACE_ID_SKY) {
+            g.has_sky = 1;
+            for (int k = 0; k < 9; k++) {
+                g.smin[k % 3] = std::min(g.smin[k % 3], v[k]);
+                g.smax[k % 3] = std::max(g.smax[k % 3], v[k]);
+            }
+        }
+    }
+    g.scale = scale;
+
+    // device upload: nodes (8 B), leaf-ordered triangle records (48 B),
+    // NTriangleID per triangle
+    const size_t nn = env->tree.children.size(), nr = env->tree.refs.size();
+    std::vector<uint2> nodes(nn);
+    for (size_t i = 0; i < nn; i++) {
+        uint32_t sbits;
+        memcpy(&sbits, &env->tree.split[i], 4);
+        nodes[i] = make_uint2(env->tree.children[i], sbits);
+    }
+    std::vector<TriRecord> leaf(nr ? nr : 1);
+    for (size_t r = 0; r < nr; r++) leaf[r] = env->tri_records[env->tree.refs[r]];
+    env->built = true;
+    if (ctx->host_only) return VRG_OK;
+    VRG_CUDA(ctx, cudaSetDevice(ctx->device));
+    VRG_CUDA(ctx, env->d_nodes.reserve(nn * sizeof(uint2)));
+    VRG_CUDA(ctx, env->d_leaf_tris.reserve(leaf.size() * sizeof(TriRecord)));
+    VRG_CUDA(ctx, env->d_tri_ids.reserve((n ? n : 1) * sizeof(int32_t)));
+    VRG_CUDA(ctx, cudaMemcpyAsync(env->d_nodes.ptr, nodes.data(), nn * sizeof(uint2),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    VRG_CUDA(ctx, cudaMemcpyAsync(env->d_leaf_tris.ptr, leaf.data(), leaf.size() * sizeof(TriRecord),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    if (n)
+        VRG_CUDA(ctx, cudaMemcpyAsync(env->d_tri_ids.ptr, env->ids.data(), n * sizeof(int32_t),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    env->built = true;
+    return VRG_OK;
+}
+
+int vrg_env_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height) {
+    if (!env || !env->built) return VRG_ERR_STATE;
+    if (nodes) *nodes = (int64_t)env->tree.children.size();
+    if (refs) *refs = (int64_t)env->tree.refs.size();
+    if (height) *height = env->tree.height;
+    return VRG_OK;
+}
+
+int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs) {
+    if (!env || !env->built) return VRG_ERR_STATE;
+    if (children) memcpy(children, env->tree.children.data(), env->tree.children.size() * 4);
+    if (split) memcpy(split, env->tree.split.data(), env->tree.split.size() * 4);
+    if (refs) memcpy(refs, env->tree.refs.data(), env->tree.refs.size() * 4);
+    return VRG_OK;
+}
+
+// TriIntersectData layout: Nx,Ny,Nz,D, NTriangleID, edges[6], cs0, cs1,
+// flags, unused (raytracer/cache/triangle/triintersectdata.go:3-22)
+int vrg_env_get_triangle(const vrg_env *env, int64_t index, void *out48) {
+    if (!env || !out48) return VRG_ERR_INVALID;
+    if (!env->built) return VRG_ERR_STATE;
+    if (index < 0 || index >= (int64_t)env->tri_records.size()) return VRG_ERR_INVALID;
+    const TriRecord &t = env->tri_records[index];
+    unsigned char *o = static_cast<unsigned char *>(out48);
+    const float head[4] = {t.nx, t.ny, t.nz, t.d};
+    const float edges[6] = {t.e0, t.e1, t.e2, t.e3, t.e4, t.e5};
+    const int drop = (int)(t.idx_drop & 3u);
+    const uint8_t tail[4] = {(uint8_t)((drop + 1) % 3), (uint8_t)((drop + 2) % 3),
+                             env->flags[index], 0};
+    memcpy(o, head, 16);
+    memcpy(o + 16, &t.id, 4);
+    memcpy(o + 20, edges, 24);
+    memcpy(o + 44, tail, 4);
+    return VRG_OK;
+}
+
+int vrg_env_bounds(const vrg_env *env, float *mins, float *maxs) {
+    if (!env || !env->built) return VRG_ERR_STATE;
+    if (mins) memcpy(mins, env->min_bound, 12);
+    if (maxs) memcpy(maxs, env->max_bound, 12);
+    return VRG_OK;
+}
+
+}  // extern "C"

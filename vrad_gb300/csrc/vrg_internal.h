@@ -1,0 +1,190 @@
+// vrg_internal.h -- host-side state behind the C ABI in include/vradgpu.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/vradgpu.h"
+#include "vrg_device.h"
+
+namespace vrg {
+
+// kd-tree SAH constants (raytracer/kdtree/constants.go:25-28)
+constexpr int kCostOfTraversal = 75;
+constexpr int kCostOfIntersection = 167;
+constexpr int kMaxTreeDepth = 21;
+constexpr uint32_t kLeaf = 3;  // KDNODE_STATE_LEAF (raytracer/cache/optimisedkdnode.go:6)
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+// Owns a device allocation.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    // (re)allocates when the capacity is too small; contents are not kept
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes && ptr) return cudaSuccess;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e == cudaSuccess) bytes = n;
+        else ptr = nullptr;
+        return e;
+    }
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct KernelStat {
+    double ms = 0.0;
+    int64_t launches = 0;
+};
+
+struct PendingTiming {
+    std::string name;
+    cudaEvent_t start, stop;
+};
+
+}  // namespace vrg
+
+struct vrg_ctx {
+    int device = 0;
+    bool host_only = false;  // created with device < 0: host algorithms only
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    mutable std::mutex mu;
+    std::string last_error;
+    bool timing = false;
+    std::map<std::string, vrg::KernelStat> stats;
+    std::vector<vrg::PendingTiming> pending;
+    std::vector<cudaEvent_t> event_pool;
+    int64_t launches = 0;
+};
+
+// Built kd tree + intersection records (host copy).
+struct HostTree {
+    std::vector<uint32_t> children;
+    std::vector<float> split;
+    std::vector<int32_t> refs;
+    int height = 0;
+};
+
+struct PatchSet {
+    // all patches, parents included, in creation order
+    std::vector<float> mins, maxs, center, area, split_dist;
+    std::vector<int32_t> face, parent, child1, child2, split_axis, leaf_index;
+    std::vector<int32_t> face_root;  // face -> root patch (or -1)
+    std::vector<int32_t> leaf_patch; // dense leaf -> patch index
+};
+
+struct vrg_env {
+    vrg_ctx *ctx = nullptr;
+    std::mutex mu;
+
+    // Environment fields (raytracer/environment.go:28-39)
+    std::vector<float> xyz;  // 9 per triangle (TriGeometryData.VertexCoordData)
+    std::vector<int32_t> ids;
+    std::vector<uint8_t> flags;
+    std::vector<float> colours;
+    std::vector<int32_t> materials;
+    float min_bound[3] = {0, 0, 0}, max_bound[3] = {0, 0, 0};
+
+    bool built = false;
+    HostTree tree;
+    std::vector<vrg::TriRecord> tri_records;  // per triangle, insertion order
+    vrg::SceneGeom geom{};                     // bounds, sky box, scale
+
+    // device scene
+    vrg::DevBuf d_nodes, d_leaf_tris, d_tri_ids, d_tri_normals;
+
+    // lights
+    std::vector<vrg_light> lights;
+    vrg::DevBuf d_lights;
+
+    // faces
+    int32_t nfaces = 0;
+    std::vector<float> f_corner, f_u, f_v, f_normal, f_luxscale, f_refl, f_base;
+    std::vector<int32_t> f_nu, f_nv, tri_face;
+    std::vector<int64_t> luxel_offset;
+    vrg::DevBuf d_faces, d_luxel_offset, d_tri_face;
+
+    // patches / transfers / bounce
+    bool have_patches = false;
+    PatchSet patches;
+    vrg::DevBuf d_patch_nodes, d_leaf_info, d_face_root;
+    bool have_transfers = false;
+    int64_t nnz = 0;
+    int32_t transfer_k = 0;
+    vrg::DevBuf d_row_ptr, d_col, d_weight;
+    vrg::DevBuf d_leaf_direct;
+    bool have_patch_direct = false;
+    vrg::DevBuf d_emit, d_total, d_partials, d_control;
+
+    // scratch for host-buffer entry points
+    vrg::DevBuf d_in0, d_in1, d_out0, d_out1, d_out2, d_counter;
+
+    // ray stream queue
+    std::vector<float> rs_start, rs_stop;
+    std::vector<int32_t> rs_skip;
+};
+
+namespace vrg {
+
+// error plumbing
+int fail(vrg_ctx *ctx, int code, const std::string &msg);
+int cuda_fail(vrg_ctx *ctx, cudaError_t e, const char *what);
+#define VRG_CUDA(ctx, call)                                  \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return vrg::cuda_fail((ctx), _e, #call); \
+    } while (0)
+
+// timing around kernel launches
+void timing_begin(vrg_ctx *ctx, const char *name, cudaEvent_t *start);
+void timing_end(vrg_ctx *ctx, const char *name, cudaEvent_t start);
+void collect_timings(vrg_ctx *ctx);
+
+// host algorithms (C++)
+void tri_intersect_format(const float *xyz9, int32_t id, uint8_t flags, TriRecord *out,
+                          uint32_t tri_index);
+void edge_equation(const float *p1, const float *p2, int c1, int c2, const float *inside,
+                   float *out3);
+void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, float *mx);
+void light_set_falloff(const vrg_light_keys &k, vrg_light &l);
+void light_parse_spot(const vrg_light_keys &k, vrg_light &l);
+int make_rect_patches(const vrg_env &env, float max_chop, float min_chop, PatchSet &out);
+
+// device launchers (trace.cu, direct.cu, transfer.cu, bounce.cu)
+DevScene scene_view(const vrg_env *env);
+int launch_occlusion_mask(vrg_env *env, const float *start, const float *stop, int64_t n,
+                          int32_t skip_id, uint32_t *mask, int32_t *hit, float *t);
+int launch_trace_closest(vrg_env *env, const float *orig, const float *dir, const float *tmin,
+                         const float *tmax, int64_t n, int32_t skip_id, int32_t *hit, float *t);
+int launch_test_lines(vrg_env *env, const float *start, const float *stop, int64_t n,
+                      int32_t skip_id, float *frac);
+int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
+                         unsigned long long *d_rays);
+int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,
+                         float *out_rgb, unsigned long long *d_rays);
+int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k);
+int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounces,
+               float *delta);
+
+}  // namespace vrg

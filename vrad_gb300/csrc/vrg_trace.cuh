@@ -1,0 +1,209 @@
+// vrg_trace.cuh -- kd-tree traversal and shadow-line visibility on the device.
+//
+// Every float operation on the bit-exact path goes through the __f*_rn
+// intrinsics, which are never fused into FMAs whatever the compiler flags,
+// so results match the float32 CPU restatement bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vrg_device.h"
+
+namespace vrg {
+
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float rsqrt_rn(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ float dot3r(float ax, float ay, float az, float bx, float by, float bz) {
+    return radd(radd(rmul(ax, bx), rmul(ay, by)), rmul(az, bz));
+}
+__device__ __forceinline__ float pick3(int a, float x, float y, float z) {
+    return a == 0 ? x : (a == 1 ? y : z);
+}
+
+constexpr int32_t kTraceIdSky = 0x01000000;
+
+// Conservative slab half-thickness for split planes: a computed hit lies
+// within a few float32 roundings of its triangle, and treating each split
+// plane as a slab 2^-17 * (scale + |origin| + 1) thick guarantees that no
+// leaf holding such a triangle is skipped.
+__device__ __forceinline__ float ray_slack(const SceneGeom &g, float ox, float oy, float oz) {
+    float om = fmaxf(fabsf(ox), fmaxf(fabsf(oy), fabsf(oz)));
+    return rmul(7.62939453125e-06f, radd(radd(g.scale, om), 1.0f));
+}
+
+// Clip [t0, t1] to the box [mn - pad, mx + pad].  NaN bounds (a zero
+// direction component with the origin on a face) leave the interval alone.
+__device__ __forceinline__ void clip_box(const float *mn, const float *mx, float pad, float ox,
+                                         float oy, float oz, float dx, float dy, float dz,
+                                         float ix, float iy, float iz, float &t0, float &t1) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float o = pick3(a, ox, oy, oz), inv = pick3(a, ix, iy, iz), d = pick3(a, dx, dy, dz);
+        float ta = rmul(rsub(rsub(mn[a], pad), o), inv);
+        float tb = rmul(rsub(radd(mx[a], pad), o), inv);
+        bool neg = signbit(d);
+        t0 = fmaxf(t0, neg ? tb : ta);
+        t1 = fminf(t1, neg ? ta : tb);
+    }
+}
+
+// Ray/triangle test (project semantics, in this operation order):
+//   den = (Nx*dx + Ny*dy) + Nz*dz ; t = (D - ((Nx*ox + Ny*oy) + Nz*oz)) / den
+//   tmin <= t < tmax ; h = o + t*d on the two kept axes
+//   b0 = (e0*h0 + e1*h1) + e2 ; b1 = (e3*h0 + e4*h1) + e5 ; b2 = (1 - b0) - b1
+//   hit iff all three are >= 0.
+// Walks the kd tree front to back.  CLOSEST=false returns the first
+// triangle found; CLOSEST=true returns the minimum t with ties to the lower
+// triangle index -- the same answer as testing every triangle.
+template <bool CLOSEST>
+__device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, float dx, float dy,
+                            float dz, float tmin, float tmax, int32_t skip, float *t_out) {
+    int32_t best = -1;
+    float best_t = __int_as_float(0x7f800000);
+    if (s.g.ntris == 0 || !(tmin <= tmax)) {
+        *t_out = best_t;
+        return -1;
+    }
+    const float ix = rdiv(1.0f, dx), iy = rdiv(1.0f, dy), iz = rdiv(1.0f, dz);
+    const float slack = ray_slack(s.g, ox, oy, oz);
+    float t0 = tmin, t1 = tmax;
+    clip_box(s.g.bmin, s.g.bmax, slack, ox, oy, oz, dx, dy, dz, ix, iy, iz, t0, t1);
+    if (!(t0 <= t1)) {
+        *t_out = best_t;
+        return -1;
+    }
+    uint32_t st_node[kStackMax];
+    float st_t0[kStackMax], st_t1[kStackMax];
+    int sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+        uint2 nd = __ldg(&s.nodes[node]);
+        uint32_t type = nd.x & 3u;
+        while (type != 3u) {
+            const float sv = __uint_as_float(nd.y);
+            const uint32_t left = nd.x >> 2;
+            const float o = pick3((int)type, ox, oy, oz), inv = pick3((int)type, ix, iy, iz);
+            const bool neg = signbit(pick3((int)type, dx, dy, dz));
+            const uint32_t nearc = neg ? left + 1 : left, farc = neg ? left : left + 1;
+            const float sd = neg ? -slack : slack;
+            const float tne = rmul(rsub(radd(sv, sd), o), inv);
+            const float tfe = rmul(rsub(rsub(sv, sd), o), inv);
+            const bool vn = !(tne < t0), vf = !(tfe > t1);
+            if (vn) {
+                if (vf && sp < kStackMax) {
+                    st_node[sp] = farc;
+                    st_t0[sp] = fmaxf(t0, tfe);
+                    st_t1[sp] = t1;
+                    sp++;
+                }
+                node = nearc;
+                t1 = fminf(t1, tne);
+            } else {
+                node = farc;
+                t0 = fmaxf(t0, tfe);
+            }
+            nd = __ldg(&s.nodes[node]);
+            type = nd.x & 3u;
+        }
+        // leaf: TriangleIndexList[start .. start+count)
+        const uint32_t start = nd.x >> 2;
+        const int cnt = (int)__uint_as_float(nd.y);
+        const float4 *rec = s.leaf_tris + 3 * (size_t)start;
+        for (int k = 0; k < cnt; k++, rec += 3) {
+            const float4 w0 = __ldg(rec);
+            const float den = dot3r(w0.x, w0.y, w0.z, dx, dy, dz);
+            const float on = dot3r(w0.x, w0.y, w0.z, ox, oy, oz);
+            const float t = rdiv(rsub(w0.w, on), den);
+            if (!(t >= tmin && t < tmax)) continue;
+            if (CLOSEST && !(t <= best_t)) continue;
+            const float4 w2 = __ldg(rec + 2);
+            if (__float_as_int(w2.z) == skip) continue;
+            const float4 w1 = __ldg(rec + 1);
+            const uint32_t idx_drop = __float_as_uint(w2.w);
+            const int drop = (int)(idx_drop & 3u);
+            // kept axes (drop+1)%3, (drop+2)%3
+            const float o0 = drop == 0 ? oy : (drop == 1 ? oz : ox);
+            const float o1 = drop == 0 ? oz : (drop == 1 ? ox : oy);
+            const float d0 = drop == 0 ? dy : (drop == 1 ? dz : dx);
+            const float d1 = drop == 0 ? dz : (drop == 1 ? dx : dy);
+            const float h0 = radd(o0, rmul(t, d0));
+            const float h1 = radd(o1, rmul(t, d1));
+            const float b0 = radd(radd(rmul(w1.x, h0), rmul(w1.y, h1)), w1.z);
+            const float b1 = radd(radd(rmul(w1.w, h0), rmul(w2.x, h1)), w2.y);
+            const float b2 = rsub(rsub(1.0f, b0), b1);
+            if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
+                const int32_t ti = (int32_t)(idx_drop >> 2);
+                if (!CLOSEST) {
+                    *t_out = t;
+                    return ti;
+                }
+                if (t < best_t || ti < best) {
+                    best = ti;
+                    best_t = t;
+                }
+            }
+        }
+        // next stacked subtree whose interval can still hold the answer
+        for (;;) {
+            if (sp == 0) {
+                *t_out = best_t;
+                return best;
+            }
+            --sp;
+            if (CLOSEST && st_t0[sp] > best_t) continue;
+            node = st_node[sp];
+            t0 = st_t0[sp];
+            t1 = st_t1[sp];
+            break;
+        }
+    }
+}
+
+// Shadow-line setup of TestLineDoesHitSky (raytracer/trace/testline.go:22-27):
+// dir = stop - start ; len = sqrt((x*x + y*y) + z*z) ; dir = dir * (1/len).
+struct Line {
+    float ox, oy, oz, dx, dy, dz, len;
+};
+__device__ __forceinline__ Line make_line(float sx, float sy, float sz, float ex, float ey,
+                                          float ez) {
+    Line L;
+    L.ox = sx;
+    L.oy = sy;
+    L.oz = sz;
+    float dx = rsub(ex, sx), dy = rsub(ey, sy), dz = rsub(ez, sz);
+    L.len = rsqrt_rn(dot3r(dx, dy, dz, dx, dy, dz));
+    const float r = rdiv(1.0f, L.len);
+    L.dx = rmul(dx, r);
+    L.dy = rmul(dy, r);
+    L.dz = rmul(dz, r);
+    return L;
+}
+
+// Occlusion with the semantics of testline.go:36-51: the closest hit on
+// [0, len) that is not skipped occludes unless it carries TRACE_ID_SKY.
+// Computed as: an any-hit query up to where the line first comes within
+// slack of the sky triangles' box (any hit there is an opaque one), then a
+// closest-hit query over the rest.  A zero-length line is not occluded.
+__device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
+    if (!(L.len > 0.0f)) return false;
+    float th;
+    if (!s.g.has_sky) return kd_trace<false>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f, L.len, skip, &th) >= 0;
+    const float ix = rdiv(1.0f, L.dx), iy = rdiv(1.0f, L.dy), iz = rdiv(1.0f, L.dz);
+    const float pad = rmul(2.0f, ray_slack(s.g, L.ox, L.oy, L.oz));
+    float ts0 = -__int_as_float(0x7f800000), ts1 = __int_as_float(0x7f800000);
+    clip_box(s.g.smin, s.g.smax, pad, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, ix, iy, iz, ts0, ts1);
+    if (!(ts0 <= ts1)) ts0 = __int_as_float(0x7f800000);
+    const float p1 = fminf(ts0, L.len);
+    if (p1 > 0.0f &&
+        kd_trace<false>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f, p1, skip, &th) >= 0)
+        return true;
+    if (!(ts0 < L.len)) return false;
+    const int32_t h =
+        kd_trace<true>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, fmaxf(ts0, 0.0f), L.len, skip, &th);
+    return h >= 0 && (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
+}
+
+}  // namespace vrg

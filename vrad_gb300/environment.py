@@ -1,0 +1,329 @@
+"""Python face of the C ABI, named after the reference's Go API.
+
+``Environment`` mirrors ``raytracer.Environment`` (raytracer/environment.go):
+AddTriangle, AddQuad, AddAxisAlignedRectangularSolid,
+SetupAccelerationStructure, Trace4Rays, GetTriangle and the ray stream;
+``test_line_does_hit_sky`` mirrors ``trace.TestLineDoesHitSky``
+(raytracer/trace/testline.go:18).  The radiosity stages the reference lacks
+(gather, transfers, bounce) are methods on the same object.  Every call goes
+through libvradgpu.so; nothing here computes a result itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+TRACE_ID_SKY = 0x01000000
+TRACE_ID_OPAQUE = 0x02000000
+TRACE_ID_STATICPROP = 0x04000000
+
+
+class Light(C.Structure):
+    """vrg_light (include/vradgpu.h)."""
+
+    _fields_ = [("type", C.c_int32), ("origin", C.c_float * 3), ("intensity", C.c_float * 3),
+                ("normal", C.c_float * 3), ("stopdot", C.c_float), ("stopdot2", C.c_float),
+                ("exponent", C.c_float), ("constant_attn", C.c_float), ("linear_attn", C.c_float),
+                ("quadratic_attn", C.c_float), ("radius", C.c_float), ("start_fade", C.c_float),
+                ("end_fade", C.c_float), ("cap_distance", C.c_float)]
+
+
+class LightKeys(C.Structure):
+    _fields_ = [("fifty_percent_distance", C.c_float), ("zero_percent_distance", C.c_float),
+                ("hard_falloff", C.c_int32), ("constant_attn", C.c_float),
+                ("linear_attn", C.c_float), ("quadratic_attn", C.c_float), ("distance", C.c_float),
+                ("inner_cone", C.c_float), ("cone", C.c_float), ("exponent", C.c_float)]
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a if shape is None else a.reshape(shape)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.vrg_ctx_create(device, C.byref(h)), None, "vrg_ctx_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vrg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self.lib.vrg_ctx_set_stream(self.h, C.c_void_p(stream_ptr or 0)), self.h, "set_stream")
+
+    def synchronize(self):
+        check(self.lib.vrg_ctx_synchronize(self.h), self.h, "synchronize")
+
+    def set_timing(self, on: bool):
+        check(self.lib.vrg_ctx_set_timing(self.h, int(on)), self.h, "set_timing")
+
+    def kernel_stats(self, name: str):
+        ms = C.c_double()
+        n = C.c_int64()
+        check(self.lib.vrg_ctx_kernel_stats(self.h, name.encode(), C.byref(ms), C.byref(n)),
+              self.h, "kernel_stats")
+        return ms.value, n.value
+
+    def reset_stats(self):
+        check(self.lib.vrg_ctx_reset_stats(self.h), self.h, "reset_stats")
+
+    def launch_count(self) -> int:
+        return int(self.lib.vrg_ctx_launch_count(self.h))
+
+
+def make_light(type_, origin, intensity, normal=(0.0, 0.0, -1.0), **keys) -> Light:
+    """Builds one light the way CreateDirectLights does for an entity:
+    ParseLightSpot / ParseLightPoint (rad/lightmap/lights.go:210-257,417-426)
+    for spot and point lights."""
+    lib = _lib.load()
+    li = Light()
+    li.type = type_
+    li.origin[:] = origin
+    li.intensity[:] = intensity
+    li.normal[:] = normal
+    li.start_fade, li.end_fade, li.cap_distance = 0.0, -1.0, 1.0e22
+    k = LightKeys()
+    for name, val in keys.items():
+        setattr(k, name, val)
+    if type_ == 2:
+        check(lib.vrg_light_parse_spot(C.byref(k), C.byref(li)), None, "parse_spot")
+    elif type_ == 1:
+        check(lib.vrg_light_parse_point(C.byref(k), C.byref(li)), None, "parse_point")
+    return li
+
+
+def light_array(lights) -> "C.Array":
+    arr = (Light * max(len(lights), 1))()
+    for i, li in enumerate(lights):
+        arr[i] = li if isinstance(li, Light) else make_light(li.type, li.origin, li.intensity,
+                                                             li.normal, **li.keys)
+    return arr
+
+
+class Environment:
+    """raytracer.Environment on the GPU."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = C.c_void_p()
+        check(self.lib.vrg_env_create(ctx.h, C.byref(h)), ctx.h, "vrg_env_create")
+        self.h = h
+        self.n_lights = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vrg_env_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _chk(self, rc, what):
+        check(rc, self.ctx.h, what)
+
+    # --- triangle soup (environment.go:41-117) ---
+    def AddTriangle(self, tid, v1, v2, v3, colour=None, flags=0, material=0):
+        vs = [_f32(v, 3) for v in (v1, v2, v3)]
+        col = None if colour is None else _f32(colour, 3)
+        self._chk(self.lib.vrg_env_add_triangle(self.h, tid, *[_p(v) for v in vs], _p(col), flags,
+                                                material), "AddTriangle")
+
+    def AddQuad(self, tid, v1, v2, v3, v4, colour=None):
+        vs = [_f32(v, 3) for v in (v1, v2, v3, v4)]
+        col = None if colour is None else _f32(colour, 3)
+        self._chk(self.lib.vrg_env_add_quad(self.h, tid, *[_p(v) for v in vs], _p(col)), "AddQuad")
+
+    def AddAxisAlignedRectangularSolid(self, tid, mins, maxs, colour=None):
+        a, b = _f32(mins, 3), _f32(maxs, 3)
+        col = None if colour is None else _f32(colour, 3)
+        self._chk(self.lib.vrg_env_add_axis_aligned_rectangular_solid(self.h, tid, _p(a), _p(b),
+                                                                      _p(col)),
+                  "AddAxisAlignedRectangularSolid")
+
+    def add_triangles(self, xyz, ids):
+        xyz = _f32(xyz, (-1, 9))
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        self._chk(self.lib.vrg_env_add_triangles(self.h, _p(xyz), _p(ids), xyz.shape[0]),
+                  "add_triangles")
+
+    def SetupAccelerationStructure(self):
+        self._chk(self.lib.vrg_env_setup_acceleration_structure(self.h),
+                  "SetupAccelerationStructure")
+
+    def num_triangles(self) -> int:
+        return int(self.lib.vrg_env_num_triangles(self.h))
+
+    def tree(self):
+        nn, nr, ht = C.c_int64(), C.c_int64(), C.c_int32()
+        self._chk(self.lib.vrg_env_tree_info(self.h, C.byref(nn), C.byref(nr), C.byref(ht)),
+                  "tree_info")
+        ch = np.zeros(nn.value, np.uint32)
+        sp = np.zeros(nn.value, np.float32)
+        refs = np.zeros(max(nr.value, 1), np.int32)
+        self._chk(self.lib.vrg_env_get_tree(self.h, _p(ch), _p(sp), _p(refs)), "get_tree")
+        return ch, sp, refs[: nr.value], ht.value
+
+    def GetTriangle(self, index) -> bytes:
+        buf = (C.c_uint8 * 48)()
+        self._chk(self.lib.vrg_env_get_triangle(self.h, index, buf), "GetTriangle")
+        return bytes(buf)
+
+    def triangle_records(self) -> np.ndarray:
+        n = self.num_triangles()
+        return np.frombuffer(b"".join(self.GetTriangle(i) for i in range(n)),
+                             dtype=np.uint32).reshape(n, 12)
+
+    # --- trace (environment.go:140, testline.go:18) ---
+    def Trace4Rays(self, origin, direction, tmin, tmax, skip_id=-1):
+        """FourRays in SoA order (x x x x y y y y z z z z)."""
+        o, d = _f32(origin, 12), _f32(direction, 12)
+        t0, t1 = _f32(tmin, 4), _f32(tmax, 4)
+        hit = np.zeros(4, np.int32)
+        dist = np.zeros(4, np.float32)
+        nrm = np.zeros(12, np.float32)
+        self._chk(self.lib.vrg_env_trace4_rays(self.h, _p(o), _p(d), _p(t0), _p(t1), skip_id,
+                                               _p(hit), _p(dist), _p(nrm)), "Trace4Rays")
+        return hit, dist, nrm
+
+    def trace_closest(self, origin, direction, tmin, tmax, skip_id=-1):
+        o, d = _f32(origin, (-1, 3)), _f32(direction, (-1, 3))
+        n = o.shape[0]
+        t0 = _f32(np.broadcast_to(np.float32(tmin) if np.isscalar(tmin) else tmin, (n,)))
+        t1 = _f32(np.broadcast_to(np.float32(tmax) if np.isscalar(tmax) else tmax, (n,)))
+        hit = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        self._chk(self.lib.vrg_env_trace_closest(self.h, _p(o), _p(d), _p(t0), _p(t1), n, skip_id,
+                                                 _p(hit), _p(t)), "trace_closest")
+        return hit, t
+
+    def test_line_does_hit_sky(self, start, stop, static_prop_to_skip=-1):
+        a, b = _f32(start, (-1, 3)), _f32(stop, (-1, 3))
+        out = np.empty(a.shape[0], np.float32)
+        self._chk(self.lib.vrg_env_test_line_does_hit_sky(self.h, _p(a), _p(b), a.shape[0],
+                                                          static_prop_to_skip, _p(out)),
+                  "TestLineDoesHitSky")
+        return out
+
+    def occlusion_mask(self, start, stop, skip_id=-1, closest=False):
+        a, b = _f32(start, (-1, 3)), _f32(stop, (-1, 3))
+        n = a.shape[0]
+        mask = np.zeros((n + 31) // 32, np.uint32)
+        hit = np.empty(n, np.int32) if closest else None
+        t = np.empty(n, np.float32) if closest else None
+        self._chk(self.lib.vrg_env_occlusion_mask(self.h, _p(a), _p(b), n, skip_id, _p(mask),
+                                                  _p(hit), _p(t)), "occlusion_mask")
+        return (mask, hit, t) if closest else mask
+
+    def AddToRayStream(self, start, stop, skip_id=-1):
+        a, b = _f32(start, 3), _f32(stop, 3)
+        self._chk(self.lib.vrg_env_add_to_ray_stream(self.h, _p(a), _p(b), skip_id),
+                  "AddToRayStream")
+
+    def FlushStreamEntry(self):
+        self._chk(self.lib.vrg_env_flush_stream_entry(self.h), "FlushStreamEntry")
+
+    def FinishRayStream(self, capacity):
+        out = np.empty(max(capacity, 1), np.float32)
+        cnt = C.c_int64()
+        self._chk(self.lib.vrg_env_finish_ray_stream(self.h, _p(out), capacity, C.byref(cnt)),
+                  "FinishRayStream")
+        return out[: cnt.value]
+
+    # --- lights / faces / gather ---
+    def set_lights(self, lights):
+        arr = light_array(lights)
+        self.n_lights = len(lights)
+        self._chk(self.lib.vrg_env_set_lights(self.h, arr, len(lights)), "set_lights")
+        return arr
+
+    def set_faces(self, lit):
+        self._faces = dict(corner=_f32(lit.corner), u=_f32(lit.u), v=_f32(lit.v),
+                           normal=_f32(lit.normal), nu=np.ascontiguousarray(lit.nu, np.int32),
+                           nv=np.ascontiguousarray(lit.nv, np.int32),
+                           luxscale=_f32(lit.luxscale), refl=_f32(lit.refl),
+                           tri_face=np.ascontiguousarray(lit.tri_face, np.int32))
+        f = self._faces
+        self._chk(self.lib.vrg_env_set_faces(self.h, lit.n_faces, _p(f["corner"]), _p(f["u"]),
+                                             _p(f["v"]), _p(f["normal"]), _p(f["nu"]),
+                                             _p(f["nv"]), _p(f["luxscale"]), _p(f["refl"]), None,
+                                             _p(f["tri_face"])), "set_faces")
+
+    def num_luxels(self) -> int:
+        return int(self.lib.vrg_env_num_luxels(self.h))
+
+    def gather_direct_light(self, supersamples=4, seed=0):
+        out = np.empty((self.num_luxels(), 3), np.float32)
+        rays = C.c_uint64()
+        self._chk(self.lib.vrg_env_gather_direct_light(self.h, supersamples, seed, _p(out),
+                                                       C.byref(rays)), "gather_direct_light")
+        return out, rays.value
+
+    def gather_points(self, pts, nrm):
+        pts, nrm = _f32(pts, (-1, 3)), _f32(nrm, (-1, 3))
+        out = np.empty_like(pts)
+        rays = C.c_uint64()
+        self._chk(self.lib.vrg_env_gather_points(self.h, _p(pts), _p(nrm), pts.shape[0], _p(out),
+                                                 C.byref(rays)), "gather_points")
+        return out, rays.value
+
+    # --- patches / transfers / bounce ---
+    def make_patches(self, max_chop=4.0, min_chop=4.0):
+        npch, nl = C.c_int64(), C.c_int64()
+        self._chk(self.lib.vrg_env_make_patches(self.h, max_chop, min_chop, C.byref(npch),
+                                                C.byref(nl)), "make_patches")
+        n = npch.value
+        P = dict(mins=np.zeros((n, 3), np.float32), maxs=np.zeros((n, 3), np.float32),
+                 center=np.zeros((n, 3), np.float32), area=np.zeros(n, np.float32),
+                 face=np.zeros(n, np.int32), parent=np.zeros(n, np.int32),
+                 child1=np.zeros(n, np.int32), child2=np.zeros(n, np.int32),
+                 split_axis=np.zeros(n, np.int32), split_dist=np.zeros(n, np.float32),
+                 leaf_index=np.zeros(n, np.int32))
+        self._chk(self.lib.vrg_env_get_patches(self.h, *[_p(P[k]) for k in (
+            "mins", "maxs", "center", "area", "face", "parent", "child1", "child2", "split_axis",
+            "split_dist", "leaf_index")]), "get_patches")
+        P["n_leaves"] = nl.value
+        return P
+
+    def make_transfers(self, dirs_local):
+        d = _f32(dirs_local, (-1, 3))
+        nnz = C.c_int64()
+        self._chk(self.lib.vrg_env_make_transfers(self.h, _p(d), d.shape[0], C.byref(nnz)),
+                  "make_transfers")
+        return nnz.value
+
+    def get_transfers(self, n_leaves, nnz):
+        row_ptr = np.zeros(n_leaves + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int32)
+        w = np.zeros(max(nnz, 1), np.float32)
+        self._chk(self.lib.vrg_env_get_transfers(self.h, _p(row_ptr), _p(col), _p(w)),
+                  "get_transfers")
+        return row_ptr, col[:nnz], w[:nnz]
+
+    def gather_patch_direct(self, n_leaves):
+        out = np.empty((n_leaves, 3), np.float32)
+        self._chk(self.lib.vrg_env_gather_patch_direct(self.h, _p(out)), "gather_patch_direct")
+        return out
+
+    def bounce_light(self, n_leaves, max_bounces=100, rel_tol=1e-3):
+        total = np.empty((n_leaves, 3), np.float32)
+        b = C.c_int32()
+        d = C.c_float()
+        self._chk(self.lib.vrg_env_bounce_light(self.h, max_bounces, rel_tol, _p(total),
+                                                C.byref(b), C.byref(d)), "bounce_light")
+        return total, b.value, d.value

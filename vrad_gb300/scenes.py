@@ -1,0 +1,268 @@
+"""Seeded synthetic scenes for the radiosity hot path.
+
+The reference's own inputs are BSP maps (``cmd/args.go:53``) that are not part
+of the project; these generators stand in for them with box rooms built the
+way ``raytracer/environment.go:77-117`` (``AddAxisAlignedRectangularSolid``)
+builds a box: six quads in the order far (z max), near (z min), left (x min),
+right (x max), top (y max), bottom (y min); each quad ``(v1,v2,v3,v4)``
+becomes triangles ``(v1,v2,v3)`` and ``(v1,v3,v4)`` with ids ``id`` and
+``id+1`` (``AddQuad``, ``environment.go:71-75``).
+
+All randomness is SplitMix64 (Steele, Lea & Flood 2014) over a counter, one
+stream per purpose, so the same seed gives the same float32 arrays on any
+machine.  No transcendental function touches a value that reaches a kernel
+except the transfer direction table, which is built once in float64 and
+handed to both the GPU path and the oracle as an input.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+TRACE_ID_SKY = 0x01000000
+TRACE_ID_OPAQUE = 0x02000000
+TRACE_ID_STATICPROP = 0x04000000
+
+EMIT_SURFACE, EMIT_POINT, EMIT_SPOTLIGHT, EMIT_SKYLIGHT, EMIT_QUAKELIGHT, EMIT_SKYAMBIENT = range(6)
+
+ROOM = 4096.0
+_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+# stream ids
+S_BOXES, S_RAYS, S_LIGHTS, S_REFL, S_SPOTDIR = 1, 2, 3, 4, 5
+
+
+def splitmix(seed: int, idx: np.ndarray) -> np.ndarray:
+    """SplitMix64 output for state ``seed + (idx+1)*gamma`` (wrapping)."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + (idx.astype(np.uint64) + np.uint64(1)) * _GAMMA
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+class Stream:
+    """Counter-based uniform stream: u = (h >> 40) * 2^-24 in [0, 1)."""
+
+    def __init__(self, seed: int, stream: int):
+        self.base = int(splitmix(seed, np.array([stream], dtype=np.uint64))[0])
+        self.pos = 0
+
+    def uniform(self, n: int, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+        h = splitmix(self.base, np.arange(self.pos, self.pos + n, dtype=np.uint64))
+        self.pos += n
+        u = (h >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
+        return np.float32(lo) + np.float32(hi - lo) * u
+
+
+def box_quads(mins, maxs):
+    """Six quads (4 x xyz) of an axis-aligned box, in the reference's order,
+    with each face's outward normal."""
+    x0, y0, z0 = (float(c) for c in mins)
+    x1, y1, z1 = (float(c) for c in maxs)
+    quads = [
+        ((x0, y1, z1), (x1, y1, z1), (x1, y0, z1), (x0, y0, z1)),  # far
+        ((x0, y1, z0), (x1, y1, z0), (x1, y0, z0), (x0, y0, z0)),  # near
+        ((x0, y1, z1), (x0, y1, z0), (x0, y0, z0), (x0, y0, z1)),  # left
+        ((x1, y1, z1), (x1, y1, z0), (x1, y0, z0), (x1, y0, z1)),  # right
+        ((x0, y1, z1), (x1, y1, z1), (x1, y1, z0), (x0, y1, z0)),  # top
+        ((x0, y0, z1), (x1, y0, z1), (x1, y0, z0), (x0, y0, z0)),  # bottom
+    ]
+    normals = [(0, 0, 1), (0, 0, -1), (-1, 0, 0), (1, 0, 0), (0, 1, 0), (0, -1, 0)]
+    return quads, normals
+
+
+@dataclass
+class TriangleSoup:
+    """What ``Environment.AddTriangle`` receives: 9 floats and an id per triangle."""
+
+    xyz: list = field(default_factory=list)
+    ids: list = field(default_factory=list)
+
+    def add_triangle(self, tid, v1, v2, v3):
+        self.xyz.append((*v1, *v2, *v3))
+        self.ids.append(tid)
+
+    def add_quad(self, tid, v1, v2, v3, v4):
+        self.add_triangle(tid, v1, v2, v3)
+        self.add_triangle(tid + 1, v1, v3, v4)
+
+    def add_box(self, tid, mins, maxs, ceiling_id=None):
+        quads, _ = box_quads(mins, maxs)
+        for k, q in enumerate(quads):
+            self.add_quad(ceiling_id if (k == 0 and ceiling_id is not None) else tid, *q)
+
+    def arrays(self):
+        xyz = np.asarray(self.xyz, dtype=np.float32).reshape(-1, 9)
+        ids = np.asarray(self.ids, dtype=np.int64).astype(np.int32)
+        return np.ascontiguousarray(xyz), np.ascontiguousarray(ids)
+
+
+def _random_boxes(rng: Stream, n: int, edge_lo: float, edge_hi: float):
+    c = rng.uniform(3 * n, 0.0, ROOM).reshape(n, 3)
+    e = rng.uniform(3 * n, edge_lo, edge_hi).reshape(n, 3)
+    half = e * np.float32(0.5)
+    mins = np.maximum(c - half, np.float32(1.0))
+    maxs = np.minimum(c + half, np.float32(ROOM - 1.0))
+    return mins.astype(np.float32), maxs.astype(np.float32)
+
+
+@dataclass
+class TraceScene:
+    xyz: np.ndarray  # (N, 9) float32
+    ids: np.ndarray  # (N,) int32
+    starts: np.ndarray  # (R, 3) float32
+    stops: np.ndarray  # (R, 3) float32
+
+
+def anyhit_scene(seed: int = 0, n_boxes: int = 1024, n_rays: int = 1 << 20,
+                 edge=(8.0, 128.0)) -> TraceScene:
+    """Box room (12 triangles) + ``n_boxes`` boxes of 12 triangles (12,300 for
+    1,024 boxes); ``n_rays`` shadow lines with both ends uniform inside the
+    room.  Every triangle is TRACE_ID_OPAQUE."""
+    soup = TriangleSoup()
+    soup.add_box(TRACE_ID_OPAQUE, (0.0, 0.0, 0.0), (ROOM, ROOM, ROOM))
+    mins, maxs = _random_boxes(Stream(seed, S_BOXES), n_boxes, *edge)
+    for b in range(n_boxes):
+        soup.add_box(TRACE_ID_OPAQUE, mins[b], maxs[b])
+    xyz, ids = soup.arrays()
+    rr = Stream(seed, S_RAYS)
+    starts = rr.uniform(3 * n_rays, 1.0, ROOM - 1.0).reshape(n_rays, 3)
+    stops = rr.uniform(3 * n_rays, 1.0, ROOM - 1.0).reshape(n_rays, 3)
+    return TraceScene(xyz, ids, np.ascontiguousarray(starts), np.ascontiguousarray(stops))
+
+
+@dataclass
+class Light:
+    type: int
+    origin: tuple
+    intensity: tuple
+    normal: tuple = (0.0, 0.0, -1.0)
+    keys: dict = field(default_factory=dict)
+
+
+@dataclass
+class LitScene:
+    xyz: np.ndarray
+    ids: np.ndarray
+    tri_face: np.ndarray  # (N,) int32 face of each triangle, -1 if not a lit face
+    corner: np.ndarray  # (F, 3)
+    u: np.ndarray  # (F, 3)
+    v: np.ndarray  # (F, 3)
+    normal: np.ndarray  # (F, 3)
+    nu: np.ndarray  # (F,) int32
+    nv: np.ndarray  # (F,) int32
+    luxscale: np.ndarray  # (F,) float32 luxels per world unit
+    refl: np.ndarray  # (F, 3) float32, clamped to 0.99
+    lights: list
+
+    @property
+    def n_faces(self):
+        return int(self.corner.shape[0])
+
+    @property
+    def n_luxels(self):
+        return int((self.nu.astype(np.int64) * self.nv).sum())
+
+    def luxel_offset(self):
+        off = np.zeros(self.n_faces + 1, dtype=np.int64)
+        np.cumsum(self.nu.astype(np.int64) * self.nv, out=off[1:])
+        return off
+
+
+def _face_record(quad, normal, spacing):
+    p = np.asarray(quad, dtype=np.float32)
+    mn, mx = p.min(axis=0), p.max(axis=0)
+    nax = int(np.argmax(np.abs(normal)))
+    a, b = (nax + 1) % 3, (nax + 2) % 3
+    corner = mn.copy()
+    u = np.zeros(3, np.float32)
+    v = np.zeros(3, np.float32)
+    u[a] = mx[a] - mn[a]
+    v[b] = mx[b] - mn[b]
+    nu = max(1, int(np.ceil(float(u[a]) / spacing)))
+    nv = max(1, int(np.ceil(float(v[b]) / spacing)))
+    return corner, u, v, np.asarray(normal, np.float32), nu, nv
+
+
+def _unit_vectors(rng: Stream, n: int) -> np.ndarray:
+    """Uniform directions by rejection from the cube, normalised in float32."""
+    out = []
+    while len(out) < n:
+        x, y, z = (float(c) for c in rng.uniform(3, -1.0, 1.0))
+        r2 = np.float32(np.float32(x * x) + np.float32(y * y)) + np.float32(z * z)
+        if 0.0 < r2 <= 1.0:
+            inv = np.float32(1.0) / np.sqrt(np.float32(r2))
+            out.append((np.float32(x) * inv, np.float32(y) * inv, np.float32(z) * inv))
+    return np.asarray(out, dtype=np.float32)
+
+
+def lit_scene(seed: int = 0, n_faces: int = 4096, spacing: float = 16.0, n_point: int = 64,
+              n_spot: int = 8, sky: bool = True, edge=(64.0, 512.0)) -> LitScene:
+    """Direct-lighting scene: ``ceil(n_faces/6)`` boxes (edges U(64,512))
+    whose first ``n_faces`` faces carry lightmaps at ``spacing`` units per
+    luxel; the room ceiling (z = 4096) is TRACE_ID_SKY.  Lights: point lights
+    with RGB U(50,500), quadratic attenuation, radius 1,024; spotlights with a
+    30/45 degree cone; one sky-ambient light over the 162 sky directions."""
+    n_boxes = (n_faces + 5) // 6
+    soup = TriangleSoup()
+    soup.add_box(TRACE_ID_OPAQUE, (0.0, 0.0, 0.0), (ROOM, ROOM, ROOM),
+                 ceiling_id=TRACE_ID_SKY if sky else None)
+    mins, maxs = _random_boxes(Stream(seed, S_BOXES), n_boxes, *edge)
+    faces = []
+    tri_face = [-1] * 12
+    for b in range(n_boxes):
+        quads, normals = box_quads(mins[b], maxs[b])
+        for k, q in enumerate(quads):
+            soup.add_quad(TRACE_ID_OPAQUE, *q)
+            f = 6 * b + k
+            if f < n_faces:
+                faces.append(_face_record(q, normals[k], spacing))
+                tri_face += [f, f]
+            else:
+                tri_face += [-1, -1]
+    xyz, ids = soup.arrays()
+    corner = np.array([f[0] for f in faces], np.float32).reshape(-1, 3)
+    u = np.array([f[1] for f in faces], np.float32).reshape(-1, 3)
+    v = np.array([f[2] for f in faces], np.float32).reshape(-1, 3)
+    nrm = np.array([f[3] for f in faces], np.float32).reshape(-1, 3)
+    nu = np.array([f[4] for f in faces], np.int32)
+    nv = np.array([f[5] for f in faces], np.int32)
+    refl = np.minimum(Stream(seed, S_REFL).uniform(3 * len(faces), 0.1, 0.8).reshape(-1, 3),
+                      np.float32(0.99))
+
+    lr = Stream(seed, S_LIGHTS)
+    lights = []
+    for _ in range(n_point):
+        o = tuple(float(c) for c in lr.uniform(3, 1.0, ROOM - 1.0))
+        it = tuple(float(c) for c in lr.uniform(3, 50.0, 500.0))
+        lights.append(Light(EMIT_POINT, o, it, keys=dict(quadratic_attn=1.0, distance=1024.0)))
+    dirs = _unit_vectors(Stream(seed, S_SPOTDIR), n_spot)
+    for i in range(n_spot):
+        o = tuple(float(c) for c in lr.uniform(3, 1.0, ROOM - 1.0))
+        it = tuple(float(c) for c in lr.uniform(3, 50.0, 500.0))
+        lights.append(Light(EMIT_SPOTLIGHT, o, it, tuple(float(c) for c in dirs[i]),
+                            keys=dict(quadratic_attn=1.0, distance=1024.0, inner_cone=30.0,
+                                      cone=45.0, exponent=1.0)))
+    if sky:
+        lights.append(Light(EMIT_SKYAMBIENT, (0.0, 0.0, 0.0), (40.0, 50.0, 70.0)))
+    return LitScene(xyz, ids, np.asarray(tri_face, np.int32), corner, u, v, nrm, nu, nv,
+                    np.full(len(faces), np.float32(1.0 / spacing), np.float32),
+                    np.ascontiguousarray(refl, dtype=np.float32), lights)
+
+
+def transfer_directions(k: int) -> np.ndarray:
+    """K cosine-weighted directions in a local frame (x, y tangent; z normal):
+    a Fibonacci lattice on the unit disk lifted by Malley's method.  Built in
+    float64 and rounded once to float32; callers pass the same table to the
+    GPU path and to the oracle."""
+    i = np.arange(k, dtype=np.float64)
+    u1 = (i + 0.5) / k
+    u2 = np.mod(i * 0.6180339887498949, 1.0)
+    r = np.sqrt(u1)
+    phi = 2.0 * np.pi * u2
+    d = np.stack([r * np.cos(phi), r * np.sin(phi), np.sqrt(1.0 - u1)], axis=1)
+    return np.ascontiguousarray(d.astype(np.float32))
