@@ -165,20 +165,16 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def _l2_copy_gbs(torch, dev):
-    """Bandwidth of a torch copy of a 24 MiB buffer that stays in L2."""
-    a = torch.empty(6 << 20, dtype=torch.float32, device=dev)
-    b = torch.empty_like(a)
-    for _ in range(5):
-        b.copy_(a)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(200):
-        b.copy_(a)
-    e1.record()
-    torch.cuda.synchronize()
-    return 2 * a.numel() * 4 * 200 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+def _l2_read_gbs(device: int):
+    """L2 read bandwidth: a 32 MiB buffer read 200 times in one launch
+    (libvrgprobe.so, built beside the product library)."""
+    from vrad_gb300 import build as vbuild
+
+    probe = C.CDLL(str(vbuild.PROBE))
+    probe.vrg_probe_l2_read_gbs.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_void_p]
+    gbs = C.c_double()
+    rc = probe.vrg_probe_l2_read_gbs(device, 32 << 20, 200, C.byref(gbs))
+    return gbs.value if rc == 0 else None
 
 
 def run_gpu(args, rank, world, local_rank):
@@ -194,7 +190,9 @@ def run_gpu(args, rank, world, local_rank):
         td.init_process_group("nccl")
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    stream = torch.cuda.current_stream()
+    # every launch (library kernels, L2 flush, events) goes to one stream
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     lib_ctx = Context(local_rank)
     lib_ctx.set_stream(stream.cuda_stream)
     lib = lib_ctx.lib
@@ -337,14 +335,16 @@ def run_gpu(args, rank, world, local_rank):
                "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
     achieved = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
     traffic = _ncu_traffic(f"ncu_{kernel}.txt")
-    l2 = _l2_copy_gbs(torch, dev)
+    torch.cuda.synchronize()
+    l2 = _l2_read_gbs(local_rank)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "peak_kind": f"{peak_kind} HBM copy",
             "kernel": kernel, "kernel_ms": round(avg_ms, 4),
             "bytes_per_ray": round(bytes_per_unit, 2),
             "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
-            "l2_copy_gbs": round(l2, 1), "l2_frac": round(achieved / l2, 4)}
+            "l2_read_gbs_measured": round(l2, 1) if l2 else None,
+            "l2_frac": round(achieved / l2, 4) if l2 else None}
     line = {
         "metric": "shadow Mrays/s (direct-light gather)" if args.workload != "anyhit"
         else "shadow Mrays/s (any-hit occlusion mask)",
@@ -369,7 +369,7 @@ def run_gpu(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="direct", choices=["direct", "anyhit"])

@@ -17,6 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libvradgpu.so"
+PROBE = OUT / "libvrgprobe.so"  # bench-only L2 bandwidth probe
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_EXACT = ["trace.cu", "direct.cu", "transfer.cu"]
@@ -36,7 +37,7 @@ def _cuda_home(nvcc: str) -> Path:
 
 
 def _sources():
-    return [CSRC / s for s in CU_EXACT + CU_FAST + CPP]
+    return [CSRC / s for s in CU_EXACT + CU_FAST + CPP + ["probe.cu"]]
 
 
 def _headers():
@@ -44,7 +45,7 @@ def _headers():
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not PROBE.exists():
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _sources() + _headers() + [Path(__file__)])
@@ -84,6 +85,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     objs = [str(OUT / (s + ".o")) for s in CU_EXACT + CU_FAST + CPP]
     run([nvcc, "-shared", *ARCH, "-o", str(tmp), *objs, "-lpthread"])
     os.replace(tmp, LIB)
+    ptmp = OUT / f"libvrgprobe.{os.getpid()}.so"
+    run([nvcc, *common, "-shared", str(CSRC / "probe.cu"), "-o", str(ptmp)])
+    os.replace(ptmp, PROBE)
     return LIB
 
 

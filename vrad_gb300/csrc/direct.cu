@@ -164,7 +164,7 @@ __device__ __forceinline__ int find_face(const int64_t *__restrict__ off, int nf
 
 // One thread per supersample; the S = 4 samples of a luxel sit in four
 // neighbouring lanes and are summed in sample order by the first of them.
-__global__ void __launch_bounds__(kThreads) k_direct_luxels(
+__global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
     float *__restrict__ out, unsigned long long *__restrict__ ray_count) {
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_luxels(
     if ((threadIdx.x & 31) == 0 && ray_count) atomicAdd(ray_count, w);
 }
 
-__global__ void __launch_bounds__(kThreads) k_direct_points(
+__global__ void __launch_bounds__(kThreads, 8) k_direct_points(
     DevScene s, const DevLight *__restrict__ lights, int nl, const float *__restrict__ pts,
     const float *__restrict__ nrm, int64_t n, float *__restrict__ out,
     unsigned long long *__restrict__ ray_count) {

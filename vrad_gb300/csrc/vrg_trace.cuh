@@ -34,17 +34,55 @@ __device__ __forceinline__ float ray_slack(const SceneGeom &g, float ox, float o
     return rmul(7.62939453125e-06f, radd(radd(g.scale, om), 1.0f));
 }
 
-// Clip [t0, t1] to the box [mn - pad, mx + pad].  NaN bounds (a zero
-// direction component with the origin on a face) leave the interval alone.
-__device__ __forceinline__ void clip_box(const float *mn, const float *mx, float pad, float ox,
-                                         float oy, float oz, float dx, float dy, float dz,
-                                         float ix, float iy, float iz, float &t0, float &t1) {
+// Approximate reciprocal for traversal decisions only.  A zero or tiny
+// direction component is replaced by +-1e-30 first, so the result is finite
+// and the slab arithmetic below never forms inf - inf.
+__device__ __forceinline__ float trav_rcp(float d) {
+    float dd = fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d;
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(dd));
+    return r;
+}
+
+// Per-ray constants of the slab walk.  For axis a with the ray moving
+// toward +a (neg = 0) the near child is the left one; a split plane s is
+// treated as the slab [s - slack, s + slack]:
+//   near child exits at  t = (s + sd - o) / d = fma(s, inv, A)
+//   far child enters at  t = (s - sd - o) / d = fma(s, inv, B)
+// with sd = +-slack toward the far side.  The rounding of these forms moves
+// a crossing by about 2^-22 * (|s| + |o|) along the axis, far inside the
+// slack, so the walk stays conservative.
+struct RayPre {
+    float inv[3], A[3], B[3];
+    uint32_t neg;  // bit a set when the direction's a component is negative
+};
+
+__device__ __forceinline__ RayPre ray_pre(float ox, float oy, float oz, float dx, float dy,
+                                          float dz, float slack) {
+    RayPre r;
+    const float o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
+    r.neg = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        float o = pick3(a, ox, oy, oz), inv = pick3(a, ix, iy, iz), d = pick3(a, dx, dy, dz);
-        float ta = rmul(rsub(rsub(mn[a], pad), o), inv);
-        float tb = rmul(rsub(radd(mx[a], pad), o), inv);
-        bool neg = signbit(d);
+        const bool neg = signbit(d[a]);
+        r.neg |= (neg ? 1u : 0u) << a;
+        r.inv[a] = trav_rcp(d[a]);
+        const float sd = neg ? -slack : slack;
+        r.A[a] = (sd - o[a]) * r.inv[a];
+        r.B[a] = (-sd - o[a]) * r.inv[a];
+    }
+    return r;
+}
+
+// Clip [t0, t1] to the box [mn - pad, mx + pad] (approximate arithmetic,
+// padded far beyond its error).
+__device__ __forceinline__ void clip_box(const float *mn, const float *mx, float pad,
+                                         const float *o, const RayPre &r, float &t0, float &t1) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float ta = ((mn[a] - pad) - o[a]) * r.inv[a];
+        const float tb = ((mx[a] + pad) - o[a]) * r.inv[a];
+        const bool neg = (r.neg >> a) & 1u;
         t0 = fmaxf(t0, neg ? tb : ta);
         t1 = fminf(t1, neg ? ta : tb);
     }
@@ -67,10 +105,13 @@ __device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, flo
         *t_out = best_t;
         return -1;
     }
-    const float ix = rdiv(1.0f, dx), iy = rdiv(1.0f, dy), iz = rdiv(1.0f, dz);
     const float slack = ray_slack(s.g, ox, oy, oz);
+    const RayPre rp = ray_pre(ox, oy, oz, dx, dy, dz, slack);
     float t0 = tmin, t1 = tmax;
-    clip_box(s.g.bmin, s.g.bmax, slack, ox, oy, oz, dx, dy, dz, ix, iy, iz, t0, t1);
+    {
+        const float o[3] = {ox, oy, oz};
+        clip_box(s.g.bmin, s.g.bmax, slack, o, rp, t0, t1);
+    }
     if (!(t0 <= t1)) {
         *t_out = best_t;
         return -1;
@@ -85,12 +126,13 @@ __device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, flo
         while (type != 3u) {
             const float sv = __uint_as_float(nd.y);
             const uint32_t left = nd.x >> 2;
-            const float o = pick3((int)type, ox, oy, oz), inv = pick3((int)type, ix, iy, iz);
-            const bool neg = signbit(pick3((int)type, dx, dy, dz));
-            const uint32_t nearc = neg ? left + 1 : left, farc = neg ? left : left + 1;
-            const float sd = neg ? -slack : slack;
-            const float tne = rmul(rsub(radd(sv, sd), o), inv);
-            const float tfe = rmul(rsub(rsub(sv, sd), o), inv);
+            const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
+            const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
+            const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
+            const uint32_t neg = (rp.neg >> type) & 1u;
+            const uint32_t nearc = left + neg, farc = left + 1u - neg;
+            const float tne = __fmaf_rn(sv, inv, A);
+            const float tfe = __fmaf_rn(sv, inv, B);
             const bool vn = !(tne < t0), vf = !(tfe > t1);
             if (vn) {
                 if (vf && sp < kStackMax) {
@@ -191,10 +233,11 @@ __device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, 
     if (!(L.len > 0.0f)) return false;
     float th;
     if (!s.g.has_sky) return kd_trace<false>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f, L.len, skip, &th) >= 0;
-    const float ix = rdiv(1.0f, L.dx), iy = rdiv(1.0f, L.dy), iz = rdiv(1.0f, L.dz);
-    const float pad = rmul(2.0f, ray_slack(s.g, L.ox, L.oy, L.oz));
+    const float pad = 2.0f * ray_slack(s.g, L.ox, L.oy, L.oz);
+    const RayPre rp = ray_pre(L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f);
     float ts0 = -__int_as_float(0x7f800000), ts1 = __int_as_float(0x7f800000);
-    clip_box(s.g.smin, s.g.smax, pad, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, ix, iy, iz, ts0, ts1);
+    const float o[3] = {L.ox, L.oy, L.oz};
+    clip_box(s.g.smin, s.g.smax, pad, o, rp, ts0, ts1);
     if (!(ts0 <= ts1)) ts0 = __int_as_float(0x7f800000);
     const float p1 = fminf(ts0, L.len);
     if (p1 > 0.0f &&
