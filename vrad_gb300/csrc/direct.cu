@@ -164,15 +164,22 @@ __device__ __forceinline__ int find_face(const int64_t *__restrict__ off, int nf
 
 // One thread per supersample; the S = 4 samples of a luxel sit in four
 // neighbouring lanes and are summed in sample order by the first of them.
+// Persistent warps take 32 samples at a time from work[0] (zeroed before
+// the launch), so faces with many occluders do not leave SMs idle.
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
-    float *__restrict__ out, unsigned long long *__restrict__ ray_count) {
+    float *__restrict__ out, unsigned long long *__restrict__ ray_count,
+    unsigned long long *__restrict__ work) {
     const int64_t nsamp = nlux * ss;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
     uint32_t rays = 0;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nsamp; base += stride) {
-        const int64_t gi = base + threadIdx.x;
+    for (;;) {
+        unsigned long long wb = 0;
+        if (lane == 0) wb = atomicAdd(work, 32ull);
+        wb = __shfl_sync(0xffffffffu, wb, 0);
+        if (wb >= (unsigned long long)nsamp) break;
+        const int64_t gi = (int64_t)wb + lane;
         float r = 0.0f, g = 0.0f, b = 0.0f;
         int64_t lux = 0;
         if (gi < nsamp) {
@@ -190,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             const float r1 = __shfl_down_sync(0xffffffffu, r, 1), r2 = __shfl_down_sync(0xffffffffu, r, 2), r3 = __shfl_down_sync(0xffffffffu, r, 3);
             const float g1 = __shfl_down_sync(0xffffffffu, g, 1), g2 = __shfl_down_sync(0xffffffffu, g, 2), g3 = __shfl_down_sync(0xffffffffu, g, 3);
             const float b1 = __shfl_down_sync(0xffffffffu, b, 1), b2 = __shfl_down_sync(0xffffffffu, b, 2), b3 = __shfl_down_sync(0xffffffffu, b, 3);
-            if (gi < nsamp && (threadIdx.x & 3) == 0) {
+            if (gi < nsamp && (lane & 3) == 0) {
                 out[3 * lux + 0] = rmul(radd(radd(radd(r, r1), r2), r3), 0.25f);
                 out[3 * lux + 1] = rmul(radd(radd(radd(g, g1), g2), g3), 0.25f);
                 out[3 * lux + 2] = rmul(radd(radd(radd(b, b1), b2), b3), 0.25f);
@@ -259,12 +266,21 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     vrg_ctx *ctx = env->ctx;
     const int64_t nlux = env->luxel_offset.empty() ? 0 : env->luxel_offset.back();
     if (nlux == 0) return VRG_OK;
+    VRG_CUDA(ctx, env->d_work.reserve(256));
+    unsigned long long *work = env->d_work.as<unsigned long long>() + 1;
+    VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_luxels, kThreads, 0) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 4;
+    const int64_t need = (nlux * ss + kThreads - 1) / kThreads;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * per_sm));
     cudaEvent_t ev = nullptr;
     timing_begin(ctx, "direct_luxels", &ev);
-    k_direct_luxels<<<grid_for(ctx, nlux * ss), kThreads, 0, ctx->stream>>>(
+    k_direct_luxels<<<grid, kThreads, 0, ctx->stream>>>(
         scene_view(env), env->d_lights.as<DevLight>(), (int)env->lights.size(),
         env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed,
-        out_rgb, d_rays);
+        out_rgb, d_rays, work);
     VRG_CUDA(ctx, cudaGetLastError());
     timing_end(ctx, "direct_luxels", ev);
     return VRG_OK;

@@ -16,18 +16,24 @@ __device__ __forceinline__ void load3(const float *p, int64_t i, float &x, float
     z = __ldg(p + 3 * i + 2);
 }
 
-// One line per thread; a warp covers 32 consecutive lines so the 1-bit mask
-// word is written with one ballot.  WANT_HIT adds the closest hit of the
-// normalised segment (hit index and t).
+// Persistent warps: each warp takes the next 32 lines from a device counter
+// (zeroed before the launch), so uneven lines balance across the GPU; the
+// 1-bit mask word of the 32 lines is written with one ballot.  WANT_HIT adds
+// the closest hit of the normalised segment (hit index and t).
 template <bool WANT_HIT>
 __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
                                                           int32_t skip, uint32_t *__restrict__ mask,
                                                           int32_t *__restrict__ hit,
-                                                          float *__restrict__ thit) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
+                                                          float *__restrict__ thit,
+                                                          unsigned long long *__restrict__ work) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(work, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned long long)n) break;
+        const int64_t i = (int64_t)base + lane;
         bool occ = false;
         if (i < n) {
             float sx, sy, sz, ex, ey, ez;
@@ -37,7 +43,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
             if (WANT_HIT) {
                 int32_t h = -1;
                 float t = __int_as_float(0x7f800000);
-                if (L.len > 0.0f) h = kd_trace<true>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f, L.len, skip, &t);
+                if (L.len > 0.0f) h = trace_ray<kClosest>(s, Ray{L.ox, L.oy, L.oz, L.dx, L.dy, L.dz}, 0.0f, L.len, skip, &t);
                 occ = h >= 0 && t < L.len && (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
                 hit[i] = h;
                 thit[i] = t;
@@ -46,7 +52,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
             }
         }
         const unsigned bits = __ballot_sync(0xffffffffu, occ);
-        if ((threadIdx.x & 31) == 0 && i < n) mask[i >> 5] = bits;
+        if (lane == 0) mask[base >> 5] = bits;
     }
 }
 
@@ -62,7 +68,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_closest(DevScene s, const fl
         load3(orig, i, ox, oy, oz);
         load3(dir, i, dx, dy, dz);
         float t;
-        hit[i] = kd_trace<true>(s, ox, oy, oz, dx, dy, dz, __ldg(tmin + i), __ldg(tmax + i), skip, &t);
+        hit[i] = trace_ray<kClosest>(s, Ray{ox, oy, oz, dx, dy, dz}, __ldg(tmin + i), __ldg(tmax + i), skip, &t);
         thit[i] = t;
     }
 }
@@ -86,6 +92,20 @@ int grid_for(const vrg_ctx *ctx, int64_t n) {
     return (int)(blocks < 1 ? 1 : blocks);
 }
 
+// Persistent grid: resident blocks per SM times SMs, but no more blocks
+// than 32-line chunks.
+template <class K>
+int persistent_grid(const vrg_ctx *ctx, K kernel, int64_t n) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 4;
+    int64_t blocks = (int64_t)ctx->num_sms * per_sm;
+    const int64_t chunks = (n + 31) / 32;
+    const int64_t need = (chunks + kThreads / 32 - 1) / (kThreads / 32);
+    if (blocks > need) blocks = need;
+    return (int)(blocks < 1 ? 1 : blocks);
+}
+
 }  // namespace
 
 DevScene scene_view(const vrg_env *env) {
@@ -102,12 +122,17 @@ int launch_occlusion_mask(vrg_env *env, const float *start, const float *stop, i
     vrg_ctx *ctx = env->ctx;
     if (n <= 0) return VRG_OK;
     DevScene s = scene_view(env);
+    VRG_CUDA(ctx, env->d_work.reserve(256));
+    unsigned long long *work = env->d_work.as<unsigned long long>();
+    VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
     cudaEvent_t ev = nullptr;
     timing_begin(ctx, "trace_mask", &ev);
     if (hit && t)
-        k_trace_mask<true><<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t);
+        k_trace_mask<true><<<persistent_grid(ctx, k_trace_mask<true>, n), kThreads, 0, ctx->stream>>>(
+            s, start, stop, n, skip_id, mask, hit, t, work);
     else
-        k_trace_mask<false><<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr);
+        k_trace_mask<false><<<persistent_grid(ctx, k_trace_mask<false>, n), kThreads, 0, ctx->stream>>>(
+            s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
     VRG_CUDA(ctx, cudaGetLastError());
     timing_end(ctx, "trace_mask", ev);
     return VRG_OK;

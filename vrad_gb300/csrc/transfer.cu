@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kRowThreads) k_transfer_rows(
             const float dy = radd(radd(rmul(lx, t1y), rmul(ly, t2y)), rmul(lz, ny));
             const float dz = radd(radd(rmul(lx, t1z), rmul(ly, t2z)), rmul(lz, nz));
             float t;
-            const int32_t h = kd_trace<true>(s, qx, qy, qz, dx, dy, dz, 0.0f, kMaxTraceLength, -1, &t);
+            const int32_t h = trace_ray<kClosest>(s, Ray{qx, qy, qz, dx, dy, dz}, 0.0f, kMaxTraceLength, -1, &t);
             int32_t target = -1;
             if (h >= 0) {
                 const int32_t g = __ldg(tri_face + h);

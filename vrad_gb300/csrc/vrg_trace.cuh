@@ -93,20 +93,28 @@ __device__ __forceinline__ void clip_box(const float *mn, const float *mx, float
 //   tmin <= t < tmax ; h = o + t*d on the two kept axes
 //   b0 = (e0*h0 + e1*h1) + e2 ; b1 = (e3*h0 + e4*h1) + e5 ; b2 = (1 - b0) - b1
 //   hit iff all three are >= 0.
-// Walks the kd tree front to back.  CLOSEST=false returns the first
-// triangle found; CLOSEST=true returns the minimum t with ties to the lower
-// triangle index -- the same answer as testing every triangle.
-template <bool CLOSEST>
-__device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, float dx, float dy,
-                            float dz, float tmin, float tmax, int32_t skip, float *t_out) {
+// Walks the kd tree front to back.  Modes:
+//   kAny      returns the first accepted triangle found;
+//   kClosest  returns the minimum t, ties to the lower triangle index -- the
+//             same answer as testing every triangle;
+//   kSkyOcc   closest-hit, except that a hit with t < any_limit returns at
+//             once (the caller guarantees no sky triangle can be hit there).
+enum TraceMode { kAny = 0, kClosest = 1, kSkyOcc = 2 };
+
+struct Ray {
+    float ox, oy, oz, dx, dy, dz;
+};
+
+template <int MODE>
+__device__ int32_t kd_trace(const DevScene &s, const Ray &ray, const RayPre &rp, float slack,
+                            float tmin, float tmax, int32_t skip, float any_limit, float *t_out) {
+    const float ox = ray.ox, oy = ray.oy, oz = ray.oz, dx = ray.dx, dy = ray.dy, dz = ray.dz;
     int32_t best = -1;
     float best_t = __int_as_float(0x7f800000);
     if (s.g.ntris == 0 || !(tmin <= tmax)) {
         *t_out = best_t;
         return -1;
     }
-    const float slack = ray_slack(s.g, ox, oy, oz);
-    const RayPre rp = ray_pre(ox, oy, oz, dx, dy, dz, slack);
     float t0 = tmin, t1 = tmax;
     {
         const float o[3] = {ox, oy, oz};
@@ -160,7 +168,7 @@ __device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, flo
             const float on = dot3r(w0.x, w0.y, w0.z, ox, oy, oz);
             const float t = rdiv(rsub(w0.w, on), den);
             if (!(t >= tmin && t < tmax)) continue;
-            if (CLOSEST && !(t <= best_t)) continue;
+            if (MODE != kAny && !(t <= best_t)) continue;
             const float4 w2 = __ldg(rec + 2);
             if (__float_as_int(w2.z) == skip) continue;
             const float4 w1 = __ldg(rec + 1);
@@ -178,7 +186,7 @@ __device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, flo
             const float b2 = rsub(rsub(1.0f, b0), b1);
             if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
                 const int32_t ti = (int32_t)(idx_drop >> 2);
-                if (!CLOSEST) {
+                if (MODE == kAny || (MODE == kSkyOcc && t < any_limit)) {
                     *t_out = t;
                     return ti;
                 }
@@ -195,13 +203,22 @@ __device__ int32_t kd_trace(const DevScene &s, float ox, float oy, float oz, flo
                 return best;
             }
             --sp;
-            if (CLOSEST && st_t0[sp] > best_t) continue;
+            if (MODE != kAny && st_t0[sp] > best_t) continue;
             node = st_node[sp];
             t0 = st_t0[sp];
             t1 = st_t1[sp];
             break;
         }
     }
+}
+
+// Closest or first hit of one ray with its own setup.
+template <int MODE>
+__device__ __forceinline__ int32_t trace_ray(const DevScene &s, const Ray &ray, float tmin,
+                                             float tmax, int32_t skip, float *t_out) {
+    const float slack = ray_slack(s.g, ray.ox, ray.oy, ray.oz);
+    const RayPre rp = ray_pre(ray.ox, ray.oy, ray.oz, ray.dx, ray.dy, ray.dz, slack);
+    return kd_trace<MODE>(s, ray, rp, slack, tmin, tmax, skip, 0.0f, t_out);
 }
 
 // Shadow-line setup of TestLineDoesHitSky (raytracer/trace/testline.go:22-27):
@@ -225,28 +242,27 @@ __device__ __forceinline__ Line make_line(float sx, float sy, float sz, float ex
 }
 
 // Occlusion with the semantics of testline.go:36-51: the closest hit on
-// [0, len) that is not skipped occludes unless it carries TRACE_ID_SKY.
-// Computed as: an any-hit query up to where the line first comes within
-// slack of the sky triangles' box (any hit there is an opaque one), then a
-// closest-hit query over the rest.  A zero-length line is not occluded.
+// [0, len) that is not skipped occludes unless it carries TRACE_ID_SKY.  The
+// walk is closest-hit, but any hit before the line first comes within
+// 2*slack of the box of the sky triangles returns at once: no sky triangle
+// can be hit there, so that hit is opaque and occludes.  A zero-length line
+// is not occluded.
 __device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
     if (!(L.len > 0.0f)) return false;
+    const Ray ray{L.ox, L.oy, L.oz, L.dx, L.dy, L.dz};
+    const float slack = ray_slack(s.g, L.ox, L.oy, L.oz);
+    const RayPre rp = ray_pre(L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, slack);
     float th;
-    if (!s.g.has_sky) return kd_trace<false>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f, L.len, skip, &th) >= 0;
-    const float pad = 2.0f * ray_slack(s.g, L.ox, L.oy, L.oz);
-    const RayPre rp = ray_pre(L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f);
+    if (!s.g.has_sky) return kd_trace<kAny>(s, ray, rp, slack, 0.0f, L.len, skip, 0.0f, &th) >= 0;
     float ts0 = -__int_as_float(0x7f800000), ts1 = __int_as_float(0x7f800000);
     const float o[3] = {L.ox, L.oy, L.oz};
-    clip_box(s.g.smin, s.g.smax, pad, o, rp, ts0, ts1);
-    if (!(ts0 <= ts1)) ts0 = __int_as_float(0x7f800000);
-    const float p1 = fminf(ts0, L.len);
-    if (p1 > 0.0f &&
-        kd_trace<false>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, 0.0f, p1, skip, &th) >= 0)
-        return true;
-    if (!(ts0 < L.len)) return false;
-    const int32_t h =
-        kd_trace<true>(s, L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, fmaxf(ts0, 0.0f), L.len, skip, &th);
-    return h >= 0 && (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
+    clip_box(s.g.smin, s.g.smax, 2.0f * slack, o, rp, ts0, ts1);
+    if (!(ts0 <= ts1) || !(ts0 < L.len)) {
+        // the line never nears a sky triangle: any hit occludes
+        return kd_trace<kAny>(s, ray, rp, slack, 0.0f, L.len, skip, 0.0f, &th) >= 0;
+    }
+    const int32_t h = kd_trace<kSkyOcc>(s, ray, rp, slack, 0.0f, L.len, skip, ts0, &th);
+    return h >= 0 && (th < ts0 || (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0);
 }
 
 }  // namespace vrg
