@@ -16,10 +16,13 @@ __device__ __forceinline__ void load3(const float *p, int64_t i, float &x, float
     z = __ldg(p + 3 * i + 2);
 }
 
-// Persistent warps: each warp takes the next 32 lines from a device counter
-// (zeroed before the launch), so uneven lines balance across the GPU; the
-// 1-bit mask word of the 32 lines is written with one ballot.  WANT_HIT adds
-// the closest hit of the normalised segment (hit index and t).
+// Shadow lines with per-lane refill.  Independent lines diverge: some stop
+// at their first leaf, some cross the whole scene.  Each lane therefore
+// walks its own line one leaf at a time, and as soon as a lane's line is
+// done the warp hands it the next unclaimed line (one atomic per refill on
+// a device counter zeroed before the launch).  The occlusion bit goes into
+// the 1-bit mask with an atomic OR (the mask is zeroed before the launch).
+// WANT_HIT also writes the closest hit of the normalised segment.
 template <bool WANT_HIT>
 __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
@@ -27,49 +30,110 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
                                                           int32_t *__restrict__ hit,
                                                           float *__restrict__ thit,
                                                           unsigned long long *__restrict__ work) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int64_t ri = 0;
+    LinePlan p;
+    TraceState st;
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(work, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= (unsigned long long)n) break;
-        const int64_t i = (int64_t)base + lane;
-        bool occ = false;
-        if (i < n) {
-            float sx, sy, sz, ex, ey, ez;
-            load3(start, i, sx, sy, sz);
-            load3(stop, i, ex, ey, ez);
-            const Line L = make_line(sx, sy, sz, ex, ey, ez);
-            if (WANT_HIT) {
-                int32_t h = -1;
-                float t = __int_as_float(0x7f800000);
-                if (L.len > 0.0f) h = trace_ray<kClosest>(s, Ray{L.ox, L.oy, L.oz, L.dx, L.dy, L.dz}, 0.0f, L.len, skip, &t);
-                occ = h >= 0 && t < L.len && (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
-                hit[i] = h;
-                thit[i] = t;
-            } else {
-                occ = line_occluded(s, L, skip);
+        const unsigned idle = __ballot_sync(full, !active && !exhausted);
+        if (idle == 0 && !__any_sync(full, active)) break;
+        if (idle) {
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(full, base, leader);
+            if (!active && !exhausted) {
+                const int64_t i = (int64_t)base + __popc(idle & below);
+                if (i >= n) {
+                    exhausted = true;
+                } else {
+                    ri = i;
+                    float sx, sy, sz, ex, ey, ez;
+                    load3(start, i, sx, sy, sz);
+                    load3(stop, i, ex, ey, ez);
+                    p = plan_line(s, make_line(sx, sy, sz, ex, ey, ez));
+                    active = !p.trivial && trace_init(s, p.ray, p.rp, p.slack, 0.0f, p.len, st);
+                    if (!active && WANT_HIT) {
+                        hit[i] = -1;
+                        thit[i] = kInf;
+                    }
+                }
             }
         }
-        const unsigned bits = __ballot_sync(0xffffffffu, occ);
-        if (lane == 0) mask[base >> 5] = bits;
+        if (active) {
+            const bool done =
+                WANT_HIT ? trace_step<kClosest>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
+                         : trace_step<kSkyOcc>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
+            if (done) {
+                active = false;
+                bool occ;
+                if (WANT_HIT) {
+                    hit[ri] = st.best;
+                    thit[ri] = st.best_t;
+                    occ = st.best >= 0 && st.best_t < p.len &&
+                          (__ldg(&s.tri_ids[st.best]) & kTraceIdSky) == 0;
+                } else {
+                    occ = line_verdict(s, p, st.best, st.best_t);
+                }
+                if (occ) atomicOr(mask + (ri >> 5), 1u << (ri & 31));
+            }
+        }
     }
 }
 
+// Closest hits of independent rays, with the same per-lane refill.
 __global__ void __launch_bounds__(kThreads) k_trace_closest(DevScene s, const float *__restrict__ orig,
                                                              const float *__restrict__ dir,
                                                              const float *__restrict__ tmin,
                                                              const float *__restrict__ tmax, int64_t n,
                                                              int32_t skip, int32_t *__restrict__ hit,
-                                                             float *__restrict__ thit) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        float ox, oy, oz, dx, dy, dz;
-        load3(orig, i, ox, oy, oz);
-        load3(dir, i, dx, dy, dz);
-        float t;
-        hit[i] = trace_ray<kClosest>(s, Ray{ox, oy, oz, dx, dy, dz}, __ldg(tmin + i), __ldg(tmax + i), skip, &t);
-        thit[i] = t;
+                                                             float *__restrict__ thit,
+                                                             unsigned long long *__restrict__ work) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int64_t ri = 0;
+    Ray ray;
+    RayPre rp;
+    float r0 = 0.0f, r1 = 0.0f;
+    TraceState st;
+    for (;;) {
+        const unsigned idle = __ballot_sync(full, !active && !exhausted);
+        if (idle == 0 && !__any_sync(full, active)) break;
+        if (idle) {
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(full, base, leader);
+            if (!active && !exhausted) {
+                const int64_t i = (int64_t)base + __popc(idle & below);
+                if (i >= n) {
+                    exhausted = true;
+                } else {
+                    ri = i;
+                    load3(orig, i, ray.ox, ray.oy, ray.oz);
+                    load3(dir, i, ray.dx, ray.dy, ray.dz);
+                    r0 = __ldg(tmin + i);
+                    r1 = __ldg(tmax + i);
+                    const float slack = ray_slack(s.g, ray.ox, ray.oy, ray.oz);
+                    rp = ray_pre(ray, slack);
+                    active = trace_init(s, ray, rp, slack, r0, r1, st);
+                    if (!active) {
+                        hit[i] = -1;
+                        thit[i] = kInf;
+                    }
+                }
+            }
+        }
+        if (active && trace_step<kClosest>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
+            active = false;
+            hit[ri] = st.best;
+            thit[ri] = st.best_t;
+        }
     }
 }
 
@@ -93,15 +157,14 @@ int grid_for(const vrg_ctx *ctx, int64_t n) {
 }
 
 // Persistent grid: resident blocks per SM times SMs, but no more blocks
-// than 32-line chunks.
+// than the rays can keep busy.
 template <class K>
 int persistent_grid(const vrg_ctx *ctx, K kernel, int64_t n) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0) != cudaSuccess || per_sm < 1)
         per_sm = 4;
     int64_t blocks = (int64_t)ctx->num_sms * per_sm;
-    const int64_t chunks = (n + 31) / 32;
-    const int64_t need = (chunks + kThreads / 32 - 1) / (kThreads / 32);
+    const int64_t need = (n + kThreads - 1) / kThreads;
     if (blocks > need) blocks = need;
     return (int)(blocks < 1 ? 1 : blocks);
 }
@@ -125,6 +188,7 @@ int launch_occlusion_mask(vrg_env *env, const float *start, const float *stop, i
     VRG_CUDA(ctx, env->d_work.reserve(256));
     unsigned long long *work = env->d_work.as<unsigned long long>();
     VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
+    VRG_CUDA(ctx, cudaMemsetAsync(mask, 0, 4 * (size_t)((n + 31) / 32), ctx->stream));
     cudaEvent_t ev = nullptr;
     timing_begin(ctx, "trace_mask", &ev);
     if (hit && t)
@@ -142,9 +206,13 @@ int launch_trace_closest(vrg_env *env, const float *orig, const float *dir, cons
                          const float *tmax, int64_t n, int32_t skip_id, int32_t *hit, float *t) {
     vrg_ctx *ctx = env->ctx;
     if (n <= 0) return VRG_OK;
+    VRG_CUDA(ctx, env->d_work.reserve(256));
+    unsigned long long *work = env->d_work.as<unsigned long long>() + 2;
+    VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
     cudaEvent_t ev = nullptr;
     timing_begin(ctx, "trace_closest", &ev);
-    k_trace_closest<<<grid_for(ctx, n), kThreads, 0, ctx->stream>>>(scene_view(env), orig, dir, tmin, tmax, n, skip_id, hit, t);
+    k_trace_closest<<<persistent_grid(ctx, k_trace_closest, n), kThreads, 0, ctx->stream>>>(
+        scene_view(env), orig, dir, tmin, tmax, n, skip_id, hit, t, work);
     VRG_CUDA(ctx, cudaGetLastError());
     timing_end(ctx, "trace_closest", ev);
     return VRG_OK;

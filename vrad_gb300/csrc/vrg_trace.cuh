@@ -1,8 +1,10 @@
 // vrg_trace.cuh -- kd-tree traversal and shadow-line visibility on the device.
 //
-// Every float operation on the bit-exact path goes through the __f*_rn
-// intrinsics, which are never fused into FMAs whatever the compiler flags,
-// so results match the float32 CPU restatement bit for bit.
+// Every float operation on the bit-exact path (the ray/triangle test, the
+// shadow-line setup) goes through the __f*_rn intrinsics, which are never
+// fused into FMAs whatever the compiler flags, so results match the float32
+// CPU restatement bit for bit.  The slab walk that only decides which leaves
+// to visit uses faster approximate arithmetic inside a conservative margin.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,6 +26,7 @@ __device__ __forceinline__ float pick3(int a, float x, float y, float z) {
 }
 
 constexpr int32_t kTraceIdSky = 0x01000000;
+constexpr float kInf = __builtin_huge_valf();
 
 // Conservative slab half-thickness for split planes: a computed hit lies
 // within a few float32 roundings of its triangle, and treating each split
@@ -44,6 +47,10 @@ __device__ __forceinline__ float trav_rcp(float d) {
     return r;
 }
 
+struct Ray {
+    float ox, oy, oz, dx, dy, dz;
+};
+
 // Per-ray constants of the slab walk.  For axis a with the ray moving
 // toward +a (neg = 0) the near child is the left one; a split plane s is
 // treated as the slab [s - slack, s + slack]:
@@ -57,10 +64,9 @@ struct RayPre {
     uint32_t neg;  // bit a set when the direction's a component is negative
 };
 
-__device__ __forceinline__ RayPre ray_pre(float ox, float oy, float oz, float dx, float dy,
-                                          float dz, float slack) {
+__device__ __forceinline__ RayPre ray_pre(const Ray &ray, float slack) {
     RayPre r;
-    const float o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
+    const float o[3] = {ray.ox, ray.oy, ray.oz}, d[3] = {ray.dx, ray.dy, ray.dz};
     r.neg = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -77,7 +83,8 @@ __device__ __forceinline__ RayPre ray_pre(float ox, float oy, float oz, float dx
 // Clip [t0, t1] to the box [mn - pad, mx + pad] (approximate arithmetic,
 // padded far beyond its error).
 __device__ __forceinline__ void clip_box(const float *mn, const float *mx, float pad,
-                                         const float *o, const RayPre &r, float &t0, float &t1) {
+                                         const Ray &ray, const RayPre &r, float &t0, float &t1) {
+    const float o[3] = {ray.ox, ray.oy, ray.oz};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const float ta = ((mn[a] - pad) - o[a]) * r.inv[a];
@@ -88,128 +95,148 @@ __device__ __forceinline__ void clip_box(const float *mn, const float *mx, float
     }
 }
 
+// Modes of a walk:
+//   kAny      stop at the first accepted triangle;
+//   kClosest  minimum t, ties to the lower triangle index -- the same answer
+//             as testing every triangle;
+//   kSkyOcc   closest-hit, except that a hit with t < any_limit stops at
+//             once (the caller guarantees no sky triangle can be hit there).
+enum TraceMode { kAny = 0, kClosest = 1, kSkyOcc = 2 };
+
+// Resumable state of one walk: the current subtree and its t interval, the
+// stack of far subtrees, and the best hit so far.
+struct TraceState {
+    uint32_t node;
+    float t0, t1;
+    int sp;
+    int32_t best;
+    float best_t;
+    uint32_t st_node[kStackMax];
+    float st_t0[kStackMax], st_t1[kStackMax];
+};
+
+// Starts a walk; returns false when the ray misses the scene's padded box
+// (st.best = -1 then).
+__device__ __forceinline__ bool trace_init(const DevScene &s, const Ray &ray, const RayPre &rp,
+                                           float slack, float tmin, float tmax, TraceState &st) {
+    st.best = -1;
+    st.best_t = kInf;
+    st.sp = 0;
+    st.node = 0;
+    if (s.g.ntris == 0 || !(tmin <= tmax)) return false;
+    st.t0 = tmin;
+    st.t1 = tmax;
+    clip_box(s.g.bmin, s.g.bmax, slack, ray, rp, st.t0, st.t1);
+    return st.t0 <= st.t1;
+}
+
 // Ray/triangle test (project semantics, in this operation order):
 //   den = (Nx*dx + Ny*dy) + Nz*dz ; t = (D - ((Nx*ox + Ny*oy) + Nz*oz)) / den
 //   tmin <= t < tmax ; h = o + t*d on the two kept axes
 //   b0 = (e0*h0 + e1*h1) + e2 ; b1 = (e3*h0 + e4*h1) + e5 ; b2 = (1 - b0) - b1
 //   hit iff all three are >= 0.
-// Walks the kd tree front to back.  Modes:
-//   kAny      returns the first accepted triangle found;
-//   kClosest  returns the minimum t, ties to the lower triangle index -- the
-//             same answer as testing every triangle;
-//   kSkyOcc   closest-hit, except that a hit with t < any_limit returns at
-//             once (the caller guarantees no sky triangle can be hit there).
-enum TraceMode { kAny = 0, kClosest = 1, kSkyOcc = 2 };
+// One step of the walk: descend to a leaf, test its triangles, pop the next
+// subtree that can still hold the answer.  Returns true when the walk is
+// over; the answer is st.best / st.best_t.
+template <int MODE>
+__device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, const RayPre &rp,
+                                           float tmin, float tmax, int32_t skip, float any_limit,
+                                           TraceState &st) {
+    const float ox = ray.ox, oy = ray.oy, oz = ray.oz, dx = ray.dx, dy = ray.dy, dz = ray.dz;
+    uint32_t node = st.node;
+    float t0 = st.t0, t1 = st.t1;
+    int sp = st.sp;
+    uint2 nd = __ldg(&s.nodes[node]);
+    uint32_t type = nd.x & 3u;
+    while (type != 3u) {
+        const float sv = __uint_as_float(nd.y);
+        const uint32_t left = nd.x >> 2;
+        const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
+        const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
+        const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
+        const uint32_t neg = (rp.neg >> type) & 1u;
+        const uint32_t nearc = left + neg, farc = left + 1u - neg;
+        const float tne = __fmaf_rn(sv, inv, A);
+        const float tfe = __fmaf_rn(sv, inv, B);
+        const bool vn = !(tne < t0), vf = !(tfe > t1);
+        if (vn) {
+            if (vf && sp < kStackMax) {
+                st.st_node[sp] = farc;
+                st.st_t0[sp] = fmaxf(t0, tfe);
+                st.st_t1[sp] = t1;
+                sp++;
+            }
+            node = nearc;
+            t1 = fminf(t1, tne);
+        } else {
+            node = farc;
+            t0 = fmaxf(t0, tfe);
+        }
+        nd = __ldg(&s.nodes[node]);
+        type = nd.x & 3u;
+    }
+    // leaf: TriangleIndexList[start .. start+count)
+    const uint32_t start = nd.x >> 2;
+    const int cnt = (int)__uint_as_float(nd.y);
+    const float4 *rec = s.leaf_tris + 3 * (size_t)start;
+    for (int k = 0; k < cnt; k++, rec += 3) {
+        const float4 w0 = __ldg(rec);
+        const float den = dot3r(w0.x, w0.y, w0.z, dx, dy, dz);
+        const float on = dot3r(w0.x, w0.y, w0.z, ox, oy, oz);
+        const float t = rdiv(rsub(w0.w, on), den);
+        if (!(t >= tmin && t < tmax)) continue;
+        if (MODE != kAny && !(t <= st.best_t)) continue;
+        const float4 w2 = __ldg(rec + 2);
+        if (__float_as_int(w2.z) == skip) continue;
+        const float4 w1 = __ldg(rec + 1);
+        const uint32_t idx_drop = __float_as_uint(w2.w);
+        const int drop = (int)(idx_drop & 3u);
+        // kept axes (drop+1)%3, (drop+2)%3
+        const float o0 = drop == 0 ? oy : (drop == 1 ? oz : ox);
+        const float o1 = drop == 0 ? oz : (drop == 1 ? ox : oy);
+        const float d0 = drop == 0 ? dy : (drop == 1 ? dz : dx);
+        const float d1 = drop == 0 ? dz : (drop == 1 ? dx : dy);
+        const float h0 = radd(o0, rmul(t, d0));
+        const float h1 = radd(o1, rmul(t, d1));
+        const float b0 = radd(radd(rmul(w1.x, h0), rmul(w1.y, h1)), w1.z);
+        const float b1 = radd(radd(rmul(w1.w, h0), rmul(w2.x, h1)), w2.y);
+        const float b2 = rsub(rsub(1.0f, b0), b1);
+        if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
+            const int32_t ti = (int32_t)(idx_drop >> 2);
+            if (MODE == kAny || (MODE == kSkyOcc && t < any_limit)) {
+                st.best = ti;
+                st.best_t = t;
+                return true;
+            }
+            if (t < st.best_t || ti < st.best) {
+                st.best = ti;
+                st.best_t = t;
+            }
+        }
+    }
+    // next stacked subtree whose interval can still hold the answer
+    for (;;) {
+        if (sp == 0) return true;
+        --sp;
+        if (MODE != kAny && st.st_t0[sp] > st.best_t) continue;
+        st.node = st.st_node[sp];
+        st.t0 = st.st_t0[sp];
+        st.t1 = st.st_t1[sp];
+        st.sp = sp;
+        return false;
+    }
+}
 
-struct Ray {
-    float ox, oy, oz, dx, dy, dz;
-};
-
+// A whole walk; returns the hit triangle index (-1 for none) and its t.
 template <int MODE>
 __device__ int32_t kd_trace(const DevScene &s, const Ray &ray, const RayPre &rp, float slack,
                             float tmin, float tmax, int32_t skip, float any_limit, float *t_out) {
-    const float ox = ray.ox, oy = ray.oy, oz = ray.oz, dx = ray.dx, dy = ray.dy, dz = ray.dz;
-    int32_t best = -1;
-    float best_t = __int_as_float(0x7f800000);
-    if (s.g.ntris == 0 || !(tmin <= tmax)) {
-        *t_out = best_t;
-        return -1;
-    }
-    float t0 = tmin, t1 = tmax;
-    {
-        const float o[3] = {ox, oy, oz};
-        clip_box(s.g.bmin, s.g.bmax, slack, o, rp, t0, t1);
-    }
-    if (!(t0 <= t1)) {
-        *t_out = best_t;
-        return -1;
-    }
-    uint32_t st_node[kStackMax];
-    float st_t0[kStackMax], st_t1[kStackMax];
-    int sp = 0;
-    uint32_t node = 0;
-    for (;;) {
-        uint2 nd = __ldg(&s.nodes[node]);
-        uint32_t type = nd.x & 3u;
-        while (type != 3u) {
-            const float sv = __uint_as_float(nd.y);
-            const uint32_t left = nd.x >> 2;
-            const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
-            const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
-            const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
-            const uint32_t neg = (rp.neg >> type) & 1u;
-            const uint32_t nearc = left + neg, farc = left + 1u - neg;
-            const float tne = __fmaf_rn(sv, inv, A);
-            const float tfe = __fmaf_rn(sv, inv, B);
-            const bool vn = !(tne < t0), vf = !(tfe > t1);
-            if (vn) {
-                if (vf && sp < kStackMax) {
-                    st_node[sp] = farc;
-                    st_t0[sp] = fmaxf(t0, tfe);
-                    st_t1[sp] = t1;
-                    sp++;
-                }
-                node = nearc;
-                t1 = fminf(t1, tne);
-            } else {
-                node = farc;
-                t0 = fmaxf(t0, tfe);
-            }
-            nd = __ldg(&s.nodes[node]);
-            type = nd.x & 3u;
+    TraceState st;
+    if (trace_init(s, ray, rp, slack, tmin, tmax, st))
+        while (!trace_step<MODE>(s, ray, rp, tmin, tmax, skip, any_limit, st)) {
         }
-        // leaf: TriangleIndexList[start .. start+count)
-        const uint32_t start = nd.x >> 2;
-        const int cnt = (int)__uint_as_float(nd.y);
-        const float4 *rec = s.leaf_tris + 3 * (size_t)start;
-        for (int k = 0; k < cnt; k++, rec += 3) {
-            const float4 w0 = __ldg(rec);
-            const float den = dot3r(w0.x, w0.y, w0.z, dx, dy, dz);
-            const float on = dot3r(w0.x, w0.y, w0.z, ox, oy, oz);
-            const float t = rdiv(rsub(w0.w, on), den);
-            if (!(t >= tmin && t < tmax)) continue;
-            if (MODE != kAny && !(t <= best_t)) continue;
-            const float4 w2 = __ldg(rec + 2);
-            if (__float_as_int(w2.z) == skip) continue;
-            const float4 w1 = __ldg(rec + 1);
-            const uint32_t idx_drop = __float_as_uint(w2.w);
-            const int drop = (int)(idx_drop & 3u);
-            // kept axes (drop+1)%3, (drop+2)%3
-            const float o0 = drop == 0 ? oy : (drop == 1 ? oz : ox);
-            const float o1 = drop == 0 ? oz : (drop == 1 ? ox : oy);
-            const float d0 = drop == 0 ? dy : (drop == 1 ? dz : dx);
-            const float d1 = drop == 0 ? dz : (drop == 1 ? dx : dy);
-            const float h0 = radd(o0, rmul(t, d0));
-            const float h1 = radd(o1, rmul(t, d1));
-            const float b0 = radd(radd(rmul(w1.x, h0), rmul(w1.y, h1)), w1.z);
-            const float b1 = radd(radd(rmul(w1.w, h0), rmul(w2.x, h1)), w2.y);
-            const float b2 = rsub(rsub(1.0f, b0), b1);
-            if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
-                const int32_t ti = (int32_t)(idx_drop >> 2);
-                if (MODE == kAny || (MODE == kSkyOcc && t < any_limit)) {
-                    *t_out = t;
-                    return ti;
-                }
-                if (t < best_t || ti < best) {
-                    best = ti;
-                    best_t = t;
-                }
-            }
-        }
-        // next stacked subtree whose interval can still hold the answer
-        for (;;) {
-            if (sp == 0) {
-                *t_out = best_t;
-                return best;
-            }
-            --sp;
-            if (MODE != kAny && st_t0[sp] > best_t) continue;
-            node = st_node[sp];
-            t0 = st_t0[sp];
-            t1 = st_t1[sp];
-            break;
-        }
-    }
+    *t_out = st.best_t;
+    return st.best;
 }
 
 // Closest or first hit of one ray with its own setup.
@@ -217,7 +244,7 @@ template <int MODE>
 __device__ __forceinline__ int32_t trace_ray(const DevScene &s, const Ray &ray, float tmin,
                                              float tmax, int32_t skip, float *t_out) {
     const float slack = ray_slack(s.g, ray.ox, ray.oy, ray.oz);
-    const RayPre rp = ray_pre(ray.ox, ray.oy, ray.oz, ray.dx, ray.dy, ray.dz, slack);
+    const RayPre rp = ray_pre(ray, slack);
     return kd_trace<MODE>(s, ray, rp, slack, tmin, tmax, skip, 0.0f, t_out);
 }
 
@@ -241,28 +268,51 @@ __device__ __forceinline__ Line make_line(float sx, float sy, float sz, float ex
     return L;
 }
 
-// Occlusion with the semantics of testline.go:36-51: the closest hit on
-// [0, len) that is not skipped occludes unless it carries TRACE_ID_SKY.  The
-// walk is closest-hit, but any hit before the line first comes within
-// 2*slack of the box of the sky triangles returns at once: no sky triangle
-// can be hit there, so that hit is opaque and occludes.  A zero-length line
-// is not occluded.
-__device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
-    if (!(L.len > 0.0f)) return false;
-    const Ray ray{L.ox, L.oy, L.oz, L.dx, L.dy, L.dz};
-    const float slack = ray_slack(s.g, L.ox, L.oy, L.oz);
-    const RayPre rp = ray_pre(L.ox, L.oy, L.oz, L.dx, L.dy, L.dz, slack);
-    float th;
-    if (!s.g.has_sky) return kd_trace<kAny>(s, ray, rp, slack, 0.0f, L.len, skip, 0.0f, &th) >= 0;
-    float ts0 = -__int_as_float(0x7f800000), ts1 = __int_as_float(0x7f800000);
-    const float o[3] = {L.ox, L.oy, L.oz};
-    clip_box(s.g.smin, s.g.smax, 2.0f * slack, o, rp, ts0, ts1);
-    if (!(ts0 <= ts1) || !(ts0 < L.len)) {
-        // the line never nears a sky triangle: any hit occludes
-        return kd_trace<kAny>(s, ray, rp, slack, 0.0f, L.len, skip, 0.0f, &th) >= 0;
+// How a shadow line is walked (semantics of testline.go:36-51: the closest
+// hit on [0, len) that is not skipped occludes unless it carries
+// TRACE_ID_SKY).  The walk is closest-hit, but any hit before the line first
+// comes within 2*slack of the box of the sky triangles stops at once: no sky
+// triangle can be hit there, so that hit is opaque and occludes.  Without
+// sky triangles near the line every hit stops the walk (any-hit).
+struct LinePlan {
+    Ray ray;
+    RayPre rp;
+    float slack, len;
+    float any_limit;  // hits before this t occlude at once (+inf: every hit)
+    bool trivial;     // zero length: not occluded, nothing to walk
+};
+
+__device__ __forceinline__ LinePlan plan_line(const DevScene &s, const Line &L) {
+    LinePlan p;
+    p.ray = Ray{L.ox, L.oy, L.oz, L.dx, L.dy, L.dz};
+    p.len = L.len;
+    p.trivial = !(L.len > 0.0f);
+    p.slack = ray_slack(s.g, L.ox, L.oy, L.oz);
+    p.rp = ray_pre(p.ray, p.slack);
+    p.any_limit = kInf;
+    if (s.g.has_sky) {
+        float ts0 = -kInf, ts1 = kInf;
+        clip_box(s.g.smin, s.g.smax, 2.0f * p.slack, p.ray, p.rp, ts0, ts1);
+        if (ts0 <= ts1 && ts0 < L.len) p.any_limit = ts0;
     }
-    const int32_t h = kd_trace<kSkyOcc>(s, ray, rp, slack, 0.0f, L.len, skip, ts0, &th);
-    return h >= 0 && (th < ts0 || (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0);
+    return p;
+}
+
+// Occlusion verdict from a finished kSkyOcc walk of a planned line.
+__device__ __forceinline__ bool line_verdict(const DevScene &s, const LinePlan &p, int32_t h,
+                                             float th) {
+    if (h < 0) return false;
+    if (th < p.any_limit) return true;
+    return (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
+}
+
+__device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
+    const LinePlan p = plan_line(s, L);
+    if (p.trivial) return false;
+    float th;
+    const int32_t h =
+        kd_trace<kSkyOcc>(s, p.ray, p.rp, p.slack, 0.0f, p.len, skip, p.any_limit, &th);
+    return line_verdict(s, p, h, th);
 }
 
 }  // namespace vrg
