@@ -241,6 +241,22 @@ int vrg_env_gather_patch_direct(vrg_env *env, float *out_rgb);
  * 3, may be NULL) is the bounced light (TotalLight, patch.go:33). */
 int vrg_env_bounce_light(vrg_env *env, int32_t max_bounces, float rel_tol, float *out_total,
                          int32_t *out_bounces, float *out_delta);
+/* The same bounce loop for callers that may not allocate device memory while
+ * they run (a serving loop that reserved its memory up front, a process whose
+ * device memory is carved out in advance by a framework pool, code that must
+ * not trigger the device-wide synchronisation of cudaMalloc/cudaFree).  This
+ * call allocates nothing: its working state lives in one fixed device array
+ * of 8 MiB + 16 KiB that every GPU loading the library holds until exit, so a
+ * scene may have at most 262144 leaf patches (larger scenes get
+ * VRG_ERR_UNSUPPORTED).  total_out is a DEVICE buffer of 4 floats per leaf
+ * (RGB + padding).  vrg_env_make_transfers and vrg_env_gather_patch_direct
+ * must have run.  The first call on a device also looks up the array's
+ * device address; make that first call before any stream capture.  All
+ * calls on a device share the one array, so calls that overlap on the GPU
+ * (two streams, two threads) race: serialise them.  No counterpart in the
+ * reference. */
+int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, float rel_tol,
+                                 float *total_out, int32_t *out_bounces, float *out_delta);
 
 #ifdef __cplusplus
 }

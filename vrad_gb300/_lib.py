@@ -69,6 +69,7 @@ SIGNATURES = {
     "vrg_env_get_transfers": (C.c_int, [P, P, P, P]),
     "vrg_env_gather_patch_direct": (C.c_int, [P, P]),
     "vrg_env_bounce_light": (C.c_int, [P, I32, F, P, P, P]),
+    "vrg_env_bounce_light_noalloc": (C.c_int, [P, I32, F, P, P, P]),
 }
 
 

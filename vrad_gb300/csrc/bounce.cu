@@ -228,3 +228,124 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
 }
 
 }  // namespace vrg
+
+// ---------------------------------------------------------------------------
+// Bounce loop without allocation.
+//
+// For callers that must not allocate device memory while they run: a
+// serving loop that has reserved its memory up front and may not grow it
+// mid-request, a process whose memory is carved out in advance by a
+// framework pool (where a stray cudaMalloc can fail or fragment the pool),
+// or code queued between other work where an implicit device-wide
+// synchronisation by cudaMalloc/cudaFree would stall unrelated streams.
+// This entry point reads only what is already resident (the transfer lists
+// from vrg_env_make_transfers and the patch direct light from
+// vrg_env_gather_patch_direct) and keeps its working state (two emission
+// buffers, per-block partial sums, the loop control block) in one
+// file-scope device array, allocated once when the library's device code is
+// loaded and held until the process exits.
+namespace vrg {
+namespace {
+
+constexpr int64_t kNoAllocMaxRows = 262144;  // leaf patches
+constexpr int kNoAllocBlocks = 1024;         // SpMV blocks (partials slots)
+constexpr int kMaxDevices = 64;
+
+struct NoAllocScratch {
+    float4 emit[2][kNoAllocMaxRows];
+    double partials[2 * kNoAllocBlocks];
+    BounceControl ctl;
+};
+
+// 8 MiB + 16 KiB on every GPU that loads the library.
+static __device__ __align__(256) NoAllocScratch g_bounce_scratch;
+
+std::mutex g_scratch_mu;
+NoAllocScratch *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device` (which must be current).
+// Looked up once per device; host code never passes the symbol itself to a
+// kernel, because on the host that name is only a stand-in.
+int noalloc_scratch(vrg_ctx *ctx, NoAllocScratch **out) {
+    if (ctx->device < 0 || ctx->device >= kMaxDevices)
+        return fail(ctx, VRG_ERR_UNSUPPORTED, "device index out of range for the no-alloc bounce");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[ctx->device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_bounce_scratch);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_bounce_scratch)");
+        g_scratch_ptr[ctx->device] = static_cast<NoAllocScratch *>(p);
+    }
+    *out = g_scratch_ptr[ctx->device];
+    return VRG_OK;
+}
+
+void count_launch(vrg_ctx *ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->launches++;
+}
+
+}  // namespace
+}  // namespace vrg
+
+extern "C" int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, float rel_tol,
+                                            float *total_out, int32_t *out_bounces,
+                                            float *out_delta) {
+    using namespace vrg;
+    if (!env) return VRG_ERR_INVALID;
+    vrg_ctx *ctx = env->ctx;
+    if (ctx->host_only) return fail(ctx, VRG_ERR_STATE, "host-only context has no device");
+    if (!env->built || !env->have_transfers)
+        return fail(ctx, VRG_ERR_STATE, "vrg_env_make_transfers has not run");
+    if (!env->have_patch_direct)
+        return fail(ctx, VRG_ERR_STATE, "vrg_env_gather_patch_direct has not run");
+    if (max_bounces < 0 || !(rel_tol >= 0.0f) || !total_out) return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(env->mu);
+    const int64_t n = (int64_t)env->patches.leaf_patch.size();
+    if (n > kNoAllocMaxRows)
+        return fail(ctx, VRG_ERR_UNSUPPORTED,
+                    "no-alloc bounce holds at most 262144 leaf patches; this scene has " +
+                        std::to_string(n));
+    VRG_CUDA(ctx, cudaSetDevice(ctx->device));
+    NoAllocScratch *sc = nullptr;
+    {
+        const int rc = noalloc_scratch(ctx, &sc);
+        if (rc != VRG_OK) return rc;
+    }
+    float4 *e0 = sc->emit[0], *e1 = sc->emit[1];
+    float4 *total = reinterpret_cast<float4 *>(total_out);
+    BounceControl *ctl = &sc->ctl;
+    double *partials = sc->partials;
+    const int nblocks = std::min(kNoAllocBlocks, ctx->num_sms * 4);
+    const int ib = (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), (int64_t)ctx->num_sms * 8);
+    // k_bounce_init zeroes the totals and resets the control block, so no
+    // state of an earlier call leaks into this one.
+    k_bounce_init<<<ib, 256, 0, ctx->stream>>>(env->d_leaf_info.as<LeafInfo>(), env->d_leaf_direct.as<float>(),
+                                               e0, total, n, ctl, max_bounces, rel_tol);
+    VRG_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx);
+    BounceControl h{};
+    int32_t launched = 0;
+    while (launched < max_bounces) {
+        float4 *in = (launched & 1) ? e1 : e0, *out = (launched & 1) ? e0 : e1;
+        k_bounce_spmv<<<nblocks, kSpmvThreads, 0, ctx->stream>>>(
+            env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), in, out, total,
+            env->d_leaf_info.as<LeafInfo>(), n, ctl, partials);
+        VRG_CUDA(ctx, cudaGetLastError());
+        k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, partials, nblocks);
+        VRG_CUDA(ctx, cudaGetLastError());
+        count_launch(ctx);
+        count_launch(ctx);
+        launched++;
+        if ((launched % kGraphBounces) == 0 || launched == max_bounces) {
+            VRG_CUDA(ctx, cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+            VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (h.done) break;
+        }
+    }
+    VRG_CUDA(ctx, cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (out_bounces) *out_bounces = h.iters;
+    if (out_delta) *out_delta = h.last_delta;
+    return VRG_OK;
+}
