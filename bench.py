@@ -435,13 +435,87 @@ def run_radiosity(args, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, local_rank):
+    """Batched bakes: 256 scenes with log-uniform face counts (64-4,096,
+    48-unit luxels, ~46M samples in all), each baked direct + bounce to a
+    1e-3 delta.  Times the batched path (one persistent direct launch + one
+    block-diagonal bounce graph) against the plain one-scene-per-launch loop
+    on the same resident scenes."""
+    import torch
+
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Batch, Context, Environment
+
+    torch.cuda.set_device(local_rank)
+    ctx = Context(local_rank)
+    t0 = time.perf_counter()
+    lits = scenes.batch_scenes(SEED, n_scenes=args.scenes)
+    dirs = scenes.transfer_directions(args.k)
+    envs = []
+    for lit in lits:
+        env = Environment(ctx)
+        env.add_triangles(lit.xyz, lit.ids)
+        env.SetupAccelerationStructure()
+        env.set_faces(lit)
+        env.set_lights(lit.lights)
+        env.make_patches()
+        env.make_transfers(dirs)
+        envs.append(env)
+    setup_s = time.perf_counter() - t0
+    batch = Batch(ctx)
+    for env in envs:
+        batch.add(env)
+
+    def plain():
+        r = 0
+        for env in envs:
+            r += env.bake(4, SEED, 100, 1e-3)
+        return r
+
+    def batched():
+        return batch.bake(4, SEED, 100, 1e-3)
+
+    res = {}
+    for name, fn in (("plain", plain), ("batched", batched)):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rays = 0
+        for _ in range(args.steps):
+            rays = fn()
+        dt = (time.perf_counter() - t0) / args.steps
+        res[name] = (dt, rays)
+    n = len(envs)
+    line = {
+        "metric": "bakes/s (batched vs one scene per launch)",
+        "value": round(n / res["batched"][0], 2), "unit": "bakes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * res["batched"][0], 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 box rooms)",
+        "config": {"workload": f"{n} scenes, faces log-uniform 64-4096, 48-unit luxels x 4 samples, "
+                               f"64-unit+ patches, {args.k} transfer rays/patch, bounce to 1e-3",
+                   "luxels": sum(l.n_luxels for l in lits), "faces": sum(l.n_faces for l in lits),
+                   "setup_s": round(setup_s, 1)},
+        "plain": {"bakes_per_s": round(n / res["plain"][0], 2), "ms_per_batch": round(1e3 * res["plain"][0], 2)},
+        "batched": {"bakes_per_s": round(n / res["batched"][0], 2),
+                    "ms_per_batch": round(1e3 * res["batched"][0], 2)},
+        "speedup": round(res["plain"][0] / res["batched"][0], 3),
+        "shadow_rays_per_batch": res["batched"][1],
+        "batched_Mrays_per_s": round(res["batched"][1] / res["batched"][0] / 1e6, 1),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="direct", choices=["direct", "anyhit", "radiosity"])
+    ap.add_argument("--workload", default="direct",
+                    choices=["direct", "anyhit", "radiosity", "batch"])
+    ap.add_argument("--scenes", type=int, default=256, help="scenes of the batch workload")
     ap.add_argument("--faces", type=int, default=4096,
                     help="lit faces of the direct-light scene (smaller only for profiling)")
     ap.add_argument("--k", type=int, default=4096, help="transfer rays per patch (radiosity)")
@@ -454,6 +528,11 @@ def main():
     elif args.workload == "radiosity":
         if rank == 0:
             run_radiosity(args, local_rank)
+    elif args.workload == "batch":
+        if rank == 0:
+            if args.k == 4096:
+                args.k = 256
+            run_batch(args, local_rank)
     else:
         run_gpu(args, rank, world, local_rank)
 

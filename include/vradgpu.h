@@ -258,6 +258,33 @@ int vrg_env_bounce_light(vrg_env *env, int32_t max_bounces, float rel_tol, float
 int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, float rel_tol,
                                  float *total_out, int32_t *out_bounces, float *out_delta);
 
+/* ------------------------------------------------------------------ */
+/* Whole bakes: one scene, or many resident scenes batched              */
+/* (RadWorld_Go's direct pass and bounce, cmd/tasks/computerad/main.go:7) */
+/* ------------------------------------------------------------------ */
+
+typedef struct vrg_batch vrg_batch;
+
+/* One scene: direct light of every luxel and leaf patch, then the bounce
+ * loop; results stay on the device (read them with vrg_env_get_bake).  The
+ * scene needs lights, faces, patches and transfers. */
+int vrg_env_bake(vrg_env *env, int32_t supersamples, uint64_t seed, int32_t max_bounces,
+                 float rel_tol, uint64_t *out_shadow_rays);
+/* Results of the last bake of this scene (any pointer may be NULL):
+ * luxel RGB, leaf-patch direct light and bounced light (3 floats each),
+ * bounces run and the final energy delta. */
+int vrg_env_get_bake(vrg_env *env, float *luxel_rgb, float *patch_direct, float *patch_total,
+                     int32_t *bounces, float *delta);
+/* A batch of resident scenes baked together: the direct pass of every
+ * scene in one persistent launch over a device work queue, then one
+ * block-diagonal bounce loop (CUDA graph) with a per-scene stop. */
+int vrg_batch_create(vrg_ctx *ctx, vrg_batch **out);
+void vrg_batch_destroy(vrg_batch *batch);
+int vrg_batch_add(vrg_batch *batch, vrg_env *env);
+int32_t vrg_batch_size(const vrg_batch *batch);
+int vrg_batch_bake(vrg_batch *batch, int32_t supersamples, uint64_t seed, int32_t max_bounces,
+                   float rel_tol, uint64_t *out_shadow_rays);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,6 +70,13 @@ SIGNATURES = {
     "vrg_env_gather_patch_direct": (C.c_int, [P, P]),
     "vrg_env_bounce_light": (C.c_int, [P, I32, F, P, P, P]),
     "vrg_env_bounce_light_noalloc": (C.c_int, [P, I32, F, P, P, P]),
+    "vrg_env_bake": (C.c_int, [P, I32, U64, I32, F, P]),
+    "vrg_env_get_bake": (C.c_int, [P, P, P, P, P, P]),
+    "vrg_batch_create": (C.c_int, [P, P]),
+    "vrg_batch_destroy": (None, [P]),
+    "vrg_batch_add": (C.c_int, [P, P]),
+    "vrg_batch_size": (I32, [P]),
+    "vrg_batch_bake": (C.c_int, [P, I32, U64, I32, F, P]),
 }
 
 

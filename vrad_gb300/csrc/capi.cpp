@@ -638,6 +638,19 @@ int vrg_env_make_patches(vrg_env *env, float max_chop, float min_chop, int64_t *
     TRY(upload(ctx, env->d_patch_nodes, nodes.data(), nodes.size() * sizeof(PatchNode)));
     TRY(upload(ctx, env->d_leaf_info, info.data(), info.size() * sizeof(LeafInfo)));
     TRY(upload(ctx, env->d_face_root, P.face_root.data(), std::max<size_t>(1, P.face_root.size()) * 4));
+    // leaf sample points for the patch direct light: centre + 0.125 * normal
+    {
+        std::vector<float> pts(3 * std::max<size_t>(nl, 1)), nrm(3 * std::max<size_t>(nl, 1));
+        for (size_t l = 0; l < nl; l++) {
+            const int32_t p = P.leaf_patch[l], f = P.face[p];
+            for (int a = 0; a < 3; a++) {
+                nrm[3 * l + a] = env->f_normal[3 * f + a];
+                pts[3 * l + a] = P.center[3 * p + a] + env->f_normal[3 * f + a] * kSampleOffset;
+            }
+        }
+        TRY(upload(ctx, env->d_patch_pts, pts.data(), pts.size() * 4));
+        TRY(upload(ctx, env->d_patch_nrm, nrm.data(), nrm.size() * 4));
+    }
     env->have_patches = true;
     env->have_transfers = env->have_patch_direct = false;
     if (num_patches) *num_patches = (int64_t)n;
@@ -692,20 +705,10 @@ int vrg_env_gather_patch_direct(vrg_env *env, float *out_rgb) {
     if (!env->have_patches) return fail(env->ctx, VRG_ERR_STATE, "MakePatches has not run");
     std::lock_guard<std::mutex> lk(env->mu);
     vrg_ctx *ctx = env->ctx;
-    const PatchSet &P = env->patches;
-    const int64_t nl = (int64_t)P.leaf_patch.size();
-    std::vector<float> pts(3 * nl), nrm(3 * nl);
-    for (int64_t l = 0; l < nl; l++) {
-        const int32_t p = P.leaf_patch[l], f = P.face[p];
-        for (int a = 0; a < 3; a++) {
-            nrm[3 * l + a] = env->f_normal[3 * f + a];
-            pts[3 * l + a] = P.center[3 * p + a] + env->f_normal[3 * f + a] * kSampleOffset;
-        }
-    }
-    TRY(upload(ctx, env->d_in0, pts.data(), 12 * nl));
-    TRY(upload(ctx, env->d_in1, nrm.data(), 12 * nl));
+    const int64_t nl = (int64_t)env->patches.leaf_patch.size();
     VRG_CUDA(ctx, env->d_leaf_direct.reserve(12 * std::max<int64_t>(nl, 1)));
-    TRY(launch_gather_points(env, env->d_in0.as<float>(), env->d_in1.as<float>(), nl, env->d_leaf_direct.as<float>(), nullptr));
+    TRY(launch_gather_points(env, env->d_patch_pts.as<float>(), env->d_patch_nrm.as<float>(), nl,
+                             env->d_leaf_direct.as<float>(), nullptr));
     if (out_rgb) TRY(download(ctx, out_rgb, env->d_leaf_direct, 12 * nl));
     TRY(sync(ctx));
     env->have_patch_direct = true;

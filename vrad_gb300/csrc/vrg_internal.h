@@ -136,6 +136,11 @@ struct vrg_env {
     vrg::DevBuf d_leaf_direct;
     bool have_patch_direct = false;
     vrg::DevBuf d_emit, d_total, d_partials, d_control;
+    vrg::DevBuf d_patch_pts, d_patch_nrm;  // leaf sample points (centre + 0.125 N), resident
+    vrg::DevBuf d_bake_rgb;                 // luxel RGB of the last bake
+    bool have_bake = false;
+    int32_t bake_bounces = 0;
+    float bake_delta = 0.0f;
 
     // scratch for host-buffer entry points
     vrg::DevBuf d_in0, d_in1, d_out0, d_out1, d_out2, d_counter;

@@ -320,6 +320,23 @@ class Environment:
         self._chk(self.lib.vrg_env_gather_patch_direct(self.h, _p(out)), "gather_patch_direct")
         return out
 
+    def bake(self, supersamples=4, seed=0, max_bounces=100, rel_tol=1e-3):
+        """Direct light + bounce of this scene (the one-scene-per-launch path)."""
+        rays = C.c_uint64()
+        self._chk(self.lib.vrg_env_bake(self.h, supersamples, seed, max_bounces, rel_tol,
+                                        C.byref(rays)), "bake")
+        return rays.value
+
+    def get_bake(self, n_leaves):
+        lux = np.empty((self.num_luxels(), 3), np.float32)
+        direct = np.empty((n_leaves, 3), np.float32)
+        total = np.empty((n_leaves, 3), np.float32)
+        b, d = C.c_int32(), C.c_float()
+        self._chk(self.lib.vrg_env_get_bake(self.h, _p(lux), _p(direct), _p(total), C.byref(b),
+                                            C.byref(d)), "get_bake")
+        return dict(luxels=lux, patch_direct=direct, patch_total=total, bounces=b.value,
+                    delta=d.value)
+
     def bounce_light(self, n_leaves, max_bounces=100, rel_tol=1e-3):
         total = np.empty((n_leaves, 3), np.float32)
         b = C.c_int32()
@@ -327,3 +344,34 @@ class Environment:
         self._chk(self.lib.vrg_env_bounce_light(self.h, max_bounces, rel_tol, _p(total),
                                                 C.byref(b), C.byref(d)), "bounce_light")
         return total, b.value, d.value
+
+
+class Batch:
+    """Resident scenes baked together (vrg_batch_*): one persistent direct
+    launch over all scenes and one block-diagonal bounce loop."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = C.c_void_p()
+        check(self.lib.vrg_batch_create(ctx.h, C.byref(h)), ctx.h, "vrg_batch_create")
+        self.h = h
+        self.envs = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vrg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def add(self, env: Environment):
+        check(self.lib.vrg_batch_add(self.h, env.h), self.ctx.h, "vrg_batch_add")
+        self.envs.append(env)
+
+    def bake(self, supersamples=4, seed=0, max_bounces=100, rel_tol=1e-3):
+        rays = C.c_uint64()
+        check(self.lib.vrg_batch_bake(self.h, supersamples, seed, max_bounces, rel_tol,
+                                      C.byref(rays)), self.ctx.h, "vrg_batch_bake")
+        return rays.value

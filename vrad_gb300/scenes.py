@@ -266,3 +266,21 @@ def transfer_directions(k: int) -> np.ndarray:
     phi = 2.0 * np.pi * u2
     d = np.stack([r * np.cos(phi), r * np.sin(phi), np.sqrt(1.0 - u1)], axis=1)
     return np.ascontiguousarray(d.astype(np.float32))
+
+
+S_BATCH = 6
+
+
+def batch_face_counts(seed: int = 0, n_scenes: int = 256, lo: int = 64, hi: int = 4096):
+    """Face counts log-uniform in [lo, hi] (uneven scene sizes)."""
+    u = Stream(seed, S_BATCH).uniform(n_scenes).astype(np.float64)
+    return np.rint(np.exp(np.log(lo) + u * (np.log(hi) - np.log(lo)))).astype(np.int64)
+
+
+def batch_scenes(seed: int = 0, n_scenes: int = 256, lo: int = 64, hi: int = 4096,
+                 spacing: float = 48.0, n_point: int = 64, n_spot: int = 8):
+    """Scenes built like the direct-light scene, with log-uniform face
+    counts; scene i uses seed 1000*seed + i + 1."""
+    counts = batch_face_counts(seed, n_scenes, lo, hi)
+    return [lit_scene(1000 * seed + i + 1, n_faces=int(c), spacing=spacing, n_point=n_point,
+                      n_spot=n_spot) for i, c in enumerate(counts)]
