@@ -285,6 +285,52 @@ int32_t vrg_batch_size(const vrg_batch *batch);
 int vrg_batch_bake(vrg_batch *batch, int32_t supersamples, uint64_t seed, int32_t max_bounces,
                    float rel_tol, uint64_t *out_shadow_rays);
 
+/* ------------------------------------------------------------------ */
+/* Relighting resident scenes, and a server for relight requests        */
+/* ------------------------------------------------------------------ */
+
+/* Replace light `index` of a scene's light table with `light`. */
+typedef struct vrg_light_edit {
+    int32_t index;
+    vrg_light light;
+} vrg_light_edit;
+
+typedef struct vrg_server vrg_server;
+
+/* Bake a scene (as vrg_env_bake) and keep, per luxel sample and leaf point,
+ * the multiplier of each sky-type light, so that later light edits re-trace
+ * only the edited point and spot lights.  Checks free device memory first
+ * (VRG_ERR_NOMEM when the scene does not fit with 1 GiB to spare). */
+int vrg_env_relight_prepare(vrg_env *env, int32_t supersamples, uint64_t seed,
+                            int32_t max_bounces, float rel_tol);
+/* Apply light edits and update the scene: luxels and leaf points of the faces
+ * within the old or new radius of an edited light are re-gathered (the same
+ * values a full gather would give), then the bounce restarts from the
+ * resident solution until the relative change falls below rel_tol or
+ * max_iters iterations.  Sky-type lights may change intensity only. */
+int vrg_env_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, int32_t max_iters,
+                    float rel_tol, int32_t *out_bounces, float *out_delta);
+/* A relight server with `slots` concurrent requests (one CUDA stream each).
+ * A worker thread admits pending requests into free slots as soon as they
+ * free up; requests on different scenes overlap on the GPU, requests on the
+ * same scene run in submission order.  A scene added to a server must only
+ * be changed through it while the server lives. */
+int vrg_server_create(vrg_ctx *ctx, int32_t slots, int32_t max_iters, float rel_tol,
+                      vrg_server **out);
+void vrg_server_destroy(vrg_server *server);
+int vrg_server_add_scene(vrg_server *server, vrg_env *env, int32_t *scene_id);
+int vrg_server_submit(vrg_server *server, int32_t scene_id, const vrg_light_edit *edits,
+                      int32_t n, int64_t *ticket);
+/* Waits for one request (returns its status: 0 done, negative error) or for
+ * every submitted request; VRG_ERR_TIMEOUT after timeout_s seconds. */
+int vrg_server_wait(vrg_server *server, int64_t ticket, double timeout_s);
+int vrg_server_drain(vrg_server *server, double timeout_s);
+/* times = {submitted, started, finished} (seconds, steady clock);
+ * digest = {sum of the scene's luxel RGB, sum of its bounced light} after
+ * the request. */
+int vrg_server_result(vrg_server *server, int64_t ticket, int32_t *status, int32_t *bounces,
+                      float *delta, double *times, double *digest);
+
 #ifdef __cplusplus
 }
 #endif

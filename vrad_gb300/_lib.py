@@ -77,6 +77,15 @@ SIGNATURES = {
     "vrg_batch_add": (C.c_int, [P, P]),
     "vrg_batch_size": (I32, [P]),
     "vrg_batch_bake": (C.c_int, [P, I32, U64, I32, F, P]),
+    "vrg_env_relight_prepare": (C.c_int, [P, I32, U64, I32, F]),
+    "vrg_env_relight": (C.c_int, [P, P, I32, I32, F, P, P]),
+    "vrg_server_create": (C.c_int, [P, I32, I32, F, P]),
+    "vrg_server_destroy": (None, [P]),
+    "vrg_server_add_scene": (C.c_int, [P, P, P]),
+    "vrg_server_submit": (C.c_int, [P, I32, P, I32, P]),
+    "vrg_server_wait": (C.c_int, [P, I64, C.c_double]),
+    "vrg_server_drain": (C.c_int, [P, C.c_double]),
+    "vrg_server_result": (C.c_int, [P, I64, P, P, P, P, P]),
 }
 
 

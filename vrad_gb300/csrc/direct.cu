@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             const int iv = (int)(local / fr.nu), iu = (int)(local - (int64_t)iv * fr.nu);
             float px, py, pz;
             luxel_sample(fr, lux, iu, iv, k, ss, seed, px, py, pz);
-            gather_point(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g, b, rays);
+            gather_point<kSkyTrace>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g, b, rays);
         }
         if (ss == 4) {
             const float r1 = __shfl_down_sync(0xffffffffu, r, 1), r2 = __shfl_down_sync(0xffffffffu, r, 2), r3 = __shfl_down_sync(0xffffffffu, r, 3);
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_points(
         const int64_t i = base + threadIdx.x;
         if (i < n) {
             float r, g, b;
-            gather_point(s, lights, nl, __ldg(pts + 3 * i), __ldg(pts + 3 * i + 1), __ldg(pts + 3 * i + 2),
+            gather_point<kSkyTrace>(s, lights, nl, __ldg(pts + 3 * i), __ldg(pts + 3 * i + 1), __ldg(pts + 3 * i + 2),
                          __ldg(nrm + 3 * i), __ldg(nrm + 3 * i + 1), __ldg(nrm + 3 * i + 2), r, g, b, rays);
             out[3 * i] = r;
             out[3 * i + 1] = g;

@@ -39,9 +39,21 @@ __device__ __forceinline__ uint64_t splitmix(uint64_t seed, uint64_t i) {
 // between start_fade and end_fade, spot cone ramp and exponent, and a
 // shadow line to the light.  Sky light: direction -normal.  Sky ambient:
 // cosine-weighted fraction of the 162 directions whose line reaches sky.
+//
+// SKY selects what happens to the sky-type lights (sky light, sky ambient),
+// which do not depend on any light position: 0 traces them; 1 traces them
+// and stores each one's multiplier (cosine or visible fraction, -1 when it
+// adds nothing) in sky[0..]; 2 reads those multipliers instead of tracing.
+// The accumulation order and arithmetic are the same in all three, so a
+// relight that re-traces only point and spot lights is bit-identical to a
+// full gather.
+enum SkyMode { kSkyTrace = 0, kSkyWrite = 1, kSkyRead = 2 };
+
+template <int SKY>
 static __device__ void gather_point(const DevScene &s, const DevLight *__restrict__ lights, int nl,
-                             float px, float py, float pz, float nx, float ny, float nz, float &r,
-                             float &g, float &b, uint32_t &rays) {
+                                    float px, float py, float pz, float nx, float ny, float nz,
+                                    float &r, float &g, float &b, uint32_t &rays,
+                                    float *__restrict__ sky = nullptr) {
     float ar = 0.0f, ag = 0.0f, ab = 0.0f;
     for (int li = 0; li < nl; li++) {
         const float4 lo = __ldg(&lights[li].origin);
@@ -88,37 +100,41 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
             ar = radd(ar, rmul(li_i.x, sc));
             ag = radd(ag, rmul(li_i.y, sc));
             ab = radd(ab, rmul(li_i.z, sc));
-        } else if (type == VRG_EMIT_SKYLIGHT) {
-            const float4 ln = __ldg(&lights[li].normal);
-            const float dx = -ln.x, dy = -ln.y, dz = -ln.z;
-            const float cosr = dot3r(nx, ny, nz, dx, dy, dz);
-            if (!(cosr > 0.0f)) continue;
-            rays++;
-            const Line L = make_line(px, py, pz, radd(px, rmul(dx, kMaxTraceLength)),
-                                     radd(py, rmul(dy, kMaxTraceLength)),
-                                     radd(pz, rmul(dz, kMaxTraceLength)));
-            if (line_occluded(s, L, -1)) continue;
-            ar = radd(ar, rmul(li_i.x, cosr));
-            ag = radd(ag, rmul(li_i.y, cosr));
-            ab = radd(ab, rmul(li_i.z, cosr));
-        } else if (type == VRG_EMIT_SKYAMBIENT) {
-            float sw = 0.0f, sv = 0.0f;
-            for (int j = 0; j < kNumAnorms; j++) {
-                const float ax = c_anorms[3 * j], ay = c_anorms[3 * j + 1], az = c_anorms[3 * j + 2];
-                const float w = dot3r(nx, ny, nz, ax, ay, az);
-                if (!(w > 0.0f)) continue;
-                sw = radd(sw, w);
-                rays++;
-                const Line L = make_line(px, py, pz, radd(px, rmul(ax, kMaxTraceLength)),
-                                         radd(py, rmul(ay, kMaxTraceLength)),
-                                         radd(pz, rmul(az, kMaxTraceLength)));
-                if (!line_occluded(s, L, -1)) sv = radd(sv, w);
+        } else if (type == VRG_EMIT_SKYLIGHT || type == VRG_EMIT_SKYAMBIENT) {
+            float m = -1.0f;  // multiplier of the intensity; -1: adds nothing
+            if (SKY == kSkyRead) {
+                m = *sky++;
+            } else if (type == VRG_EMIT_SKYLIGHT) {
+                const float4 ln = __ldg(&lights[li].normal);
+                const float dx = -ln.x, dy = -ln.y, dz = -ln.z;
+                const float cosr = dot3r(nx, ny, nz, dx, dy, dz);
+                if (cosr > 0.0f) {
+                    rays++;
+                    const Line L = make_line(px, py, pz, radd(px, rmul(dx, kMaxTraceLength)),
+                                             radd(py, rmul(dy, kMaxTraceLength)),
+                                             radd(pz, rmul(dz, kMaxTraceLength)));
+                    if (!line_occluded(s, L, -1)) m = cosr;
+                }
+            } else {
+                float sw = 0.0f, sv = 0.0f;
+                for (int j = 0; j < kNumAnorms; j++) {
+                    const float ax = c_anorms[3 * j], ay = c_anorms[3 * j + 1], az = c_anorms[3 * j + 2];
+                    const float w = dot3r(nx, ny, nz, ax, ay, az);
+                    if (!(w > 0.0f)) continue;
+                    sw = radd(sw, w);
+                    rays++;
+                    const Line L = make_line(px, py, pz, radd(px, rmul(ax, kMaxTraceLength)),
+                                             radd(py, rmul(ay, kMaxTraceLength)),
+                                             radd(pz, rmul(az, kMaxTraceLength)));
+                    if (!line_occluded(s, L, -1)) sv = radd(sv, w);
+                }
+                if (sw > 0.0f) m = rdiv(sv, sw);
             }
-            if (sw > 0.0f) {
-                const float fr = rdiv(sv, sw);
-                ar = radd(ar, rmul(li_i.x, fr));
-                ag = radd(ag, rmul(li_i.y, fr));
-                ab = radd(ab, rmul(li_i.z, fr));
+            if (SKY == kSkyWrite) *sky++ = m;
+            if (m >= 0.0f) {
+                ar = radd(ar, rmul(li_i.x, m));
+                ag = radd(ag, rmul(li_i.y, m));
+                ab = radd(ab, rmul(li_i.z, m));
             }
         }
     }

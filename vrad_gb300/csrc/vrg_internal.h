@@ -142,6 +142,15 @@ struct vrg_env {
     int32_t bake_bounces = 0;
     float bake_delta = 0.0f;
 
+    // relighting: sky multipliers cached per sample, warm-start bounce state
+    bool relight_ready = false;
+    int32_t relight_ss = 4;
+    uint64_t relight_seed = 0;
+    int32_t sky_slots = 0;
+    vrg::DevBuf d_sky_lux, d_sky_pts, d_emit0, d_x;
+    std::vector<float> face_lo, face_hi;      // face bounds (3 floats each)
+    std::vector<int32_t> face_leaf_begin;     // leaves of face f: [begin[f], begin[f+1])
+
     // scratch for host-buffer entry points
     vrg::DevBuf d_in0, d_in1, d_out0, d_out1, d_out2, d_counter;
     vrg::DevBuf d_work;  // work-queue counters of the persistent kernels
@@ -189,6 +198,7 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
                          unsigned long long *d_rays);
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,
                          float *out_rgb, unsigned long long *d_rays);
+void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst);
 int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k);
 int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounces,
                float *delta);

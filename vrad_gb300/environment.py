@@ -327,6 +327,18 @@ class Environment:
                                         C.byref(rays)), "bake")
         return rays.value
 
+    def relight_prepare(self, supersamples=4, seed=0, max_bounces=100, rel_tol=1e-3):
+        self._chk(self.lib.vrg_env_relight_prepare(self.h, supersamples, seed, max_bounces,
+                                                   rel_tol), "relight_prepare")
+
+    def relight(self, edits, max_iters=32, rel_tol=1e-3):
+        """edits: [(light index, Light)]; returns (bounces, delta)."""
+        arr = edit_array(edits)
+        b, d = C.c_int32(), C.c_float()
+        self._chk(self.lib.vrg_env_relight(self.h, arr, len(edits), max_iters, rel_tol,
+                                           C.byref(b), C.byref(d)), "relight")
+        return b.value, d.value
+
     def get_bake(self, n_leaves):
         lux = np.empty((self.num_luxels(), 3), np.float32)
         direct = np.empty((n_leaves, 3), np.float32)
@@ -344,6 +356,70 @@ class Environment:
         self._chk(self.lib.vrg_env_bounce_light(self.h, max_bounces, rel_tol, _p(total),
                                                 C.byref(b), C.byref(d)), "bounce_light")
         return total, b.value, d.value
+
+
+class LightEdit(C.Structure):
+    """vrg_light_edit: replace light `index` with `light`."""
+
+    _fields_ = [("index", C.c_int32), ("light", Light)]
+
+
+def edit_array(edits) -> "C.Array":
+    arr = (LightEdit * max(len(edits), 1))()
+    for i, (idx, li) in enumerate(edits):
+        arr[i].index = idx
+        arr[i].light = li if isinstance(li, Light) else make_light(li.type, li.origin,
+                                                                   li.intensity, li.normal,
+                                                                   **li.keys)
+    return arr
+
+
+class Server:
+    """Relight server (vrg_server_*): slots requests in flight at once, one
+    CUDA stream each, admitted as slots and scenes free up."""
+
+    def __init__(self, ctx: Context, slots=8, max_iters=32, rel_tol=1e-3):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = C.c_void_p()
+        check(self.lib.vrg_server_create(ctx.h, slots, max_iters, rel_tol, C.byref(h)), ctx.h,
+              "vrg_server_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vrg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_scene(self, env: Environment) -> int:
+        sid = C.c_int32()
+        check(self.lib.vrg_server_add_scene(self.h, env.h, C.byref(sid)), self.ctx.h, "add_scene")
+        return sid.value
+
+    def submit(self, scene: int, edits) -> int:
+        arr = edit_array(edits)
+        t = C.c_int64()
+        check(self.lib.vrg_server_submit(self.h, scene, arr, len(edits), C.byref(t)), self.ctx.h,
+              "submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout=60.0) -> int:
+        return int(self.lib.vrg_server_wait(self.h, ticket, timeout))
+
+    def drain(self, timeout=600.0):
+        check(self.lib.vrg_server_drain(self.h, timeout), self.ctx.h, "drain")
+
+    def result(self, ticket: int) -> dict:
+        st, b, d = C.c_int32(), C.c_int32(), C.c_float()
+        times = (C.c_double * 3)()
+        dig = (C.c_double * 2)()
+        check(self.lib.vrg_server_result(self.h, ticket, C.byref(st), C.byref(b), C.byref(d), times,
+                                         dig), self.ctx.h, "result")
+        return dict(status=st.value, bounces=b.value, delta=d.value, submit=times[0],
+                    start=times[1], done=times[2], digest=(dig[0], dig[1]))
 
 
 class Batch:
