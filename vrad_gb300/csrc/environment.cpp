@@ -105,7 +105,8 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     }
     g.scale = scale;
 
-    // device upload: nodes (8 B), leaf-ordered triangle records (48 B),
+    // device upload: nodes (8 B), then in TriangleIndexList order the
+    // triangle planes (16 B each) followed by the edge parts (32 B each),
     // NTriangleID per triangle
     const size_t nn = env->tree.children.size(), nr = env->tree.refs.size();
     std::vector<uint2> nodes(nn);
@@ -114,17 +115,26 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         memcpy(&sbits, &env->tree.split[i], 4);
         nodes[i] = make_uint2(env->tree.children[i], sbits);
     }
-    std::vector<TriRecord> leaf(nr ? nr : 1);
-    for (size_t r = 0; r < nr; r++) leaf[r] = env->tri_records[env->tree.refs[r]];
+    const size_t nr1 = nr ? nr : 1;
+    std::vector<float4> leaf(3 * nr1, make_float4(0, 0, 0, 0));
+    for (size_t r = 0; r < nr; r++) {
+        const TriRecord &t = env->tri_records[env->tree.refs[r]];
+        float id_bits, idx_bits;
+        memcpy(&id_bits, &t.id, 4);
+        memcpy(&idx_bits, &t.idx_drop, 4);
+        leaf[r] = make_float4(t.nx, t.ny, t.nz, t.d);
+        leaf[nr1 + 2 * r] = make_float4(t.e0, t.e1, t.e2, t.e3);
+        leaf[nr1 + 2 * r + 1] = make_float4(t.e4, t.e5, id_bits, idx_bits);
+    }
     env->built = true;
     if (ctx->host_only) return VRG_OK;
     VRG_CUDA(ctx, cudaSetDevice(ctx->device));
     VRG_CUDA(ctx, env->d_nodes.reserve(nn * sizeof(uint2)));
-    VRG_CUDA(ctx, env->d_leaf_tris.reserve(leaf.size() * sizeof(TriRecord)));
+    VRG_CUDA(ctx, env->d_leaf_tris.reserve(leaf.size() * sizeof(float4)));
     VRG_CUDA(ctx, env->d_tri_ids.reserve((n ? n : 1) * sizeof(int32_t)));
     VRG_CUDA(ctx, cudaMemcpyAsync(env->d_nodes.ptr, nodes.data(), nn * sizeof(uint2),
                                   cudaMemcpyHostToDevice, ctx->stream));
-    VRG_CUDA(ctx, cudaMemcpyAsync(env->d_leaf_tris.ptr, leaf.data(), leaf.size() * sizeof(TriRecord),
+    VRG_CUDA(ctx, cudaMemcpyAsync(env->d_leaf_tris.ptr, leaf.data(), leaf.size() * sizeof(float4),
                                   cudaMemcpyHostToDevice, ctx->stream));
     if (n)
         VRG_CUDA(ctx, cudaMemcpyAsync(env->d_tri_ids.ptr, env->ids.data(), n * sizeof(int32_t),

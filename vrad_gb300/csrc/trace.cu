@@ -65,8 +65,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
         }
         if (active) {
             const bool done =
-                WANT_HIT ? trace_step<kClosest>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
-                         : trace_step<kSkyOcc>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
+                WANT_HIT ? trace_step<kClosest, 4>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
+                         : trace_step<kSkyOcc, 4>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
             if (done) {
                 active = false;
                 bool occ;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_closest(DevScene s, const fl
                 }
             }
         }
-        if (active && trace_step<kClosest>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
+        if (active && trace_step<kClosest, 4>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
             active = false;
             hit[ri] = st.best;
             thit[ri] = st.best_t;
@@ -174,7 +174,8 @@ int persistent_grid(const vrg_ctx *ctx, K kernel, int64_t n) {
 DevScene scene_view(const vrg_env *env) {
     DevScene s;
     s.nodes = env->d_nodes.as<uint2>();
-    s.leaf_tris = env->d_leaf_tris.as<float4>();
+    s.leaf_planes = env->d_leaf_tris.as<float4>();
+    s.leaf_edges = s.leaf_planes + std::max<size_t>(env->tree.refs.size(), 1);
     s.tri_ids = env->d_tri_ids.as<int32_t>();
     s.g = env->geom;
     return s;

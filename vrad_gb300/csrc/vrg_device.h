@@ -36,11 +36,15 @@ struct SceneGeom {
     int64_t ntris;
 };
 
-// Device view of a resident scene.
+// Device view of a resident scene.  The triangle records of the leaves are
+// split in two arrays indexed by TriangleIndexList position: the plane
+// (Nx, Ny, Nz, D), which the test reads first and which rejects most
+// triangles, and the edge part (e0..e3), (e4, e5, id, index<<2 | drop).
 struct DevScene {
-    const uint2 *nodes;       // (children, split bits) per kd node
-    const float4 *leaf_tris;  // 3 float4 per TriangleIndexList entry
-    const int32_t *tri_ids;   // NTriangleID per triangle index
+    const uint2 *nodes;         // (children, split bits) per kd node
+    const float4 *leaf_planes;  // 1 float4 per TriangleIndexList entry
+    const float4 *leaf_edges;   // 2 float4 per TriangleIndexList entry
+    const int32_t *tri_ids;     // NTriangleID per triangle index
     SceneGeom g;
 };
 

@@ -137,8 +137,10 @@ __device__ __forceinline__ bool trace_init(const DevScene &s, const Ray &ray, co
 //   hit iff all three are >= 0.
 // One step of the walk: descend to a leaf, test its triangles, pop the next
 // subtree that can still hold the answer.  Returns true when the walk is
-// over; the answer is st.best / st.best_t.
-template <int MODE>
+// over; the answer is st.best / st.best_t.  LB triangle planes are fetched
+// at a time so their loads overlap (more registers; latency-bound walks of
+// incoherent rays gain, register-capped gathers use 1).
+template <int MODE, int LB = 1>
 __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, const RayPre &rp,
                                            float tmin, float tmax, int32_t skip, float any_limit,
                                            TraceState &st) {
@@ -178,17 +180,28 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
     // leaf: TriangleIndexList[start .. start+count)
     const uint32_t start = nd.x >> 2;
     const int cnt = (int)__uint_as_float(nd.y);
-    const float4 *rec = s.leaf_tris + 3 * (size_t)start;
-    for (int k = 0; k < cnt; k++, rec += 3) {
-        const float4 w0 = __ldg(rec);
+    // planes are fetched LB at a time so their loads overlap; the edge part
+    // is fetched only for triangles whose plane hit is in range
+    constexpr int kLeafBatch = LB;
+    const float4 *pl = s.leaf_planes + start;
+    const float4 *ed = s.leaf_edges + 2 * (size_t)start;
+    for (int k0 = 0; k0 < cnt; k0 += kLeafBatch) {
+        float4 P[kLeafBatch];
+#pragma unroll
+        for (int j = 0; j < kLeafBatch; j++)
+            if (k0 + j < cnt) P[j] = __ldg(pl + k0 + j);
+#pragma unroll
+        for (int j = 0; j < kLeafBatch; j++) {
+        if (k0 + j >= cnt) break;
+        const float4 w0 = P[j];
         const float den = dot3r(w0.x, w0.y, w0.z, dx, dy, dz);
         const float on = dot3r(w0.x, w0.y, w0.z, ox, oy, oz);
         const float t = rdiv(rsub(w0.w, on), den);
         if (!(t >= tmin && t < tmax)) continue;
         if (MODE != kAny && !(t <= st.best_t)) continue;
-        const float4 w2 = __ldg(rec + 2);
+        const float4 w2 = __ldg(ed + 2 * (k0 + j) + 1);
         if (__float_as_int(w2.z) == skip) continue;
-        const float4 w1 = __ldg(rec + 1);
+        const float4 w1 = __ldg(ed + 2 * (k0 + j));
         const uint32_t idx_drop = __float_as_uint(w2.w);
         const int drop = (int)(idx_drop & 3u);
         // kept axes (drop+1)%3, (drop+2)%3
@@ -212,6 +225,7 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
                 st.best = ti;
                 st.best_t = t;
             }
+        }
         }
     }
     // next stacked subtree whose interval can still hold the answer
