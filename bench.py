@@ -345,6 +345,9 @@ def run_gpu(args, rank, world, local_rank):
             "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
             "l2_read_gbs_measured": round(l2, 1) if l2 else None,
             "l2_frac": round(achieved / l2, 4) if l2 else None}
+    tkey = (Context.tune_key("trace_mask", env.num_triangles(), n) if args.workload == "anyhit"
+            else Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
+    tv, tms = lib_ctx.autotune_choice(tkey)
     line = {
         "metric": "shadow Mrays/s (direct-light gather)" if args.workload != "anyhit"
         else "shadow Mrays/s (any-hit occlusion mask)",
@@ -353,7 +356,9 @@ def run_gpu(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 box rooms)",
         "config": {"workload": workload, "rays_per_step": units,
-                   "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}"},
+                   "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",
+                   "autotune": {"bucket": tkey, "variant": tv,
+                                "variant_ms": [round(x, 4) for x in tms]}},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

@@ -104,6 +104,20 @@ int vrg_ctx_reset_stats(vrg_ctx *ctx);
 /* Kernels launched by this context since creation (all names). */
 int64_t vrg_ctx_launch_count(const vrg_ctx *ctx);
 
+/* Per-scene-size autotuning (no reference counterpart).  Tuned launch
+ * sites ("trace_mask", "trace_mask_hit", "direct_luxels") offer variants
+ * that give identical results; the first launch in a bucket
+ * "<site>/t<log2 triangles>/n<log2 work items>" times each once on the real
+ * input and keeps the fastest.  On by default; off, or inside a stream
+ * capture, an untuned bucket runs variant 0. */
+int vrg_ctx_set_autotune(vrg_ctx *ctx, int enable);
+/* The variant chosen for `key` (-1 if untuned) and, when `ms` is not NULL,
+ * up to `cap` per-variant times of the tuning run. */
+int vrg_ctx_autotune_choice(vrg_ctx *ctx, const char *key, int32_t *variant, double *ms, int32_t cap);
+/* Save / load the tuned choices as text lines "key variant". */
+int vrg_ctx_autotune_save(vrg_ctx *ctx, const char *path);
+int vrg_ctx_autotune_load(vrg_ctx *ctx, const char *path);
+
 /* ------------------------------------------------------------------ */
 /* Environment: raytracer/environment.go                                */
 /* ------------------------------------------------------------------ */

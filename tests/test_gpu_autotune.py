@@ -1,0 +1,77 @@
+"""Autotuned launch sites: every variant gives the same bits, the first
+launch in a bucket records a choice with one time per variant, and a saved
+choice loads back."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal, small_lit_scene
+
+
+def _force(ctx, tmp_path, key, variant):
+    p = tmp_path / f"tune_{variant}.txt"
+    p.write_text(f"{key} {variant}\n")
+    ctx.autotune_load(str(p))
+    assert ctx.autotune_choice(key)[0] == variant
+
+
+def test_tune_file_round_trip_host(host_ctx, tmp_path):
+    from vrad_gb300.environment import Context
+
+    key = Context.tune_key("trace_mask", 12300, 1 << 20)
+    assert key == "trace_mask/t13/n20"
+    assert Context.tune_key("direct_luxels", 1, 0) == "direct_luxels/t0/n0"
+    assert host_ctx.autotune_choice("nope/t1/n1")[0] == -1
+    _force(host_ctx, tmp_path, key, 2)
+    out = tmp_path / "saved.txt"
+    host_ctx.autotune_save(str(out))
+    assert f"{key} 2" in out.read_text().splitlines()
+    # out-of-range variants in a file are ignored
+    bad = tmp_path / "bad.txt"
+    bad.write_text("trace_mask/t1/n1 99\n")
+    host_ctx.autotune_load(str(bad))
+    assert host_ctx.autotune_choice("trace_mask/t1/n1")[0] == -1
+
+
+@pytest.mark.gpu
+def test_trace_mask_variants_identical(gpu_ctx, anyhit_scene, tmp_path):
+    from vrad_gb300.environment import Context, Environment
+
+    sc = anyhit_scene
+    env = Environment(gpu_ctx)
+    env.add_triangles(sc.xyz, sc.ids)
+    env.SetupAccelerationStructure()
+    n = 1 << 15
+    a, b = sc.starts[:n], sc.stops[:n]
+    for closest in (False, True):
+        key = Context.tune_key("trace_mask_hit" if closest else "trace_mask", env.num_triangles(), n)
+        outs = []
+        for v in range(3):
+            _force(gpu_ctx, tmp_path, key, v)
+            outs.append(env.occlusion_mask(a, b, closest=closest))
+        for o in outs[1:]:
+            if closest:
+                assert all(bits_equal(x, y) for x, y in zip(o, outs[0]))
+            else:
+                assert np.array_equal(o, outs[0])
+
+
+@pytest.mark.gpu
+def test_direct_variants_identical_and_choice_recorded(gpu_ctx, tmp_path):
+    from vrad_gb300.environment import Context, Environment
+
+    lit = small_lit_scene(64, seed=11)
+    env = Environment(gpu_ctx)
+    env.add_triangles(lit.xyz, lit.ids)
+    env.SetupAccelerationStructure()
+    env.set_faces(lit)
+    env.set_lights(lit.lights)
+    key = Context.tune_key("direct_luxels", env.num_triangles(), env.num_luxels() * 4)
+    assert gpu_ctx.autotune_choice(key)[0] == -1
+    rgb0, rays0 = env.gather_direct_light(supersamples=4, seed=2)  # tunes this bucket
+    v, ms = gpu_ctx.autotune_choice(key)
+    assert v in (0, 1, 2) and len(ms) == 3
+    for v in range(3):
+        _force(gpu_ctx, tmp_path, key, v)
+        rgb, rays = env.gather_direct_light(supersamples=4, seed=2)
+        assert rays == rays0
+        assert bits_equal(rgb, rgb0)

@@ -150,12 +150,13 @@ def test_device_entry_point_and_launch_count(env0, oscene0, anyhit_scene, gpu_ct
     a = torch.from_numpy(sc.starts[:n]).cuda()
     b = torch.from_numpy(sc.stops[:n]).cuda()
     m = torch.zeros((n + 31) // 32, dtype=torch.int32, device="cuda")
-    before = gpu_ctx.launch_count()
     torch.cuda.synchronize()
-    rc = env0.lib.vrg_env_occlusion_mask_d(env0.h, a.data_ptr(), b.data_ptr(), n, -1,
-                                           m.data_ptr(), None, None)
-    assert rc == 0
-    gpu_ctx.synchronize()
+    for _ in range(2):  # the first call in a size bucket may time every variant
+        before = gpu_ctx.launch_count()
+        rc = env0.lib.vrg_env_occlusion_mask_d(env0.h, a.data_ptr(), b.data_ptr(), n, -1,
+                                               m.data_ptr(), None, None)
+        assert rc == 0
+        gpu_ctx.synchronize()
     assert gpu_ctx.launch_count() == before + 1
     ref = oscene0.occlusion_mask(sc.starts[:n], sc.stops[:n], threads=16)
     assert np.array_equal(m.cpu().numpy().view(np.uint32), ref)

@@ -33,6 +33,10 @@ SIGNATURES = {
     "vrg_ctx_kernel_stats": (C.c_int, [P, C.c_char_p, P, P]),
     "vrg_ctx_reset_stats": (C.c_int, [P]),
     "vrg_ctx_launch_count": (I64, [P]),
+    "vrg_ctx_set_autotune": (C.c_int, [P, C.c_int]),
+    "vrg_ctx_autotune_choice": (C.c_int, [P, C.c_char_p, P, P, I32]),
+    "vrg_ctx_autotune_save": (C.c_int, [P, C.c_char_p]),
+    "vrg_ctx_autotune_load": (C.c_int, [P, C.c_char_p]),
     "vrg_env_create": (C.c_int, [P, P]),
     "vrg_env_destroy": (None, [P]),
     "vrg_env_add_triangle": (C.c_int, [P, I32, P, P, P, P, C.c_uint16, I32]),

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_EXACT = ["trace.cu", "direct.cu", "transfer.cu", "batch.cu", "relight.cu"]
 CU_FAST = ["bounce.cu"]
-CPP = ["capi.cpp", "environment.cpp", "kdbuild.cpp", "lights.cpp", "patches.cpp"]
+CPP = ["capi.cpp", "environment.cpp", "kdbuild.cpp", "lights.cpp", "patches.cpp", "tune.cpp"]
 
 
 def _nvcc() -> str:

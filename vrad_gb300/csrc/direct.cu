@@ -20,8 +20,10 @@ constexpr int kThreads = 128;
 
 // One thread per supersample; the S = 4 samples of a luxel sit in four
 // neighbouring lanes and are summed in sample order by the first of them.
-// Persistent warps take 32 samples at a time from work[0] (zeroed before
-// the launch), so faces with many occluders do not leave SMs idle.
+// Persistent warps take FETCH samples at a time from work[0] (zeroed before
+// the launch), so faces with many occluders do not leave SMs idle; larger
+// claims mean fewer atomics, smaller ones a shorter tail.
+template <int FETCH>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
@@ -31,9 +33,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     const int lane = threadIdx.x & 31;
     uint32_t rays = 0;
     for (;;) {
-        unsigned long long wb = 0;
-        if (lane == 0) wb = atomicAdd(work, 32ull);
-        wb = __shfl_sync(0xffffffffu, wb, 0);
+        unsigned long long wb0 = 0;
+        if (lane == 0) wb0 = atomicAdd(work, (unsigned long long)FETCH);
+        wb0 = __shfl_sync(0xffffffffu, wb0, 0);
+        if (wb0 >= (unsigned long long)nsamp) break;
+        for (int sub = 0; sub < FETCH; sub += 32) {
+        const unsigned long long wb = wb0 + sub;
         if (wb >= (unsigned long long)nsamp) break;
         const int64_t gi = (int64_t)wb + lane;
         float r = 0.0f, g = 0.0f, b = 0.0f;
@@ -62,6 +67,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             out[3 * lux + 0] = r;
             out[3 * lux + 1] = g;
             out[3 * lux + 2] = b;
+        }
         }
     }
     // one atomic per warp
@@ -124,22 +130,33 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     if (nlux == 0) return VRG_OK;
     VRG_CUDA(ctx, env->d_work.reserve(256));
     unsigned long long *work = env->d_work.as<unsigned long long>() + 1;
-    VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_luxels, kThreads, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_luxels<32>, kThreads, 0) != cudaSuccess ||
         per_sm < 1)
         per_sm = 4;
     const int64_t need = (nlux * ss + kThreads - 1) / kThreads;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * per_sm));
-    cudaEvent_t ev = nullptr;
-    timing_begin(ctx, "direct_luxels", &ev);
-    k_direct_luxels<<<grid, kThreads, 0, ctx->stream>>>(
-        scene_view(env), env->d_lights.as<DevLight>(), (int)env->lights.size(),
-        env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed,
-        out_rgb, d_rays, work);
-    VRG_CUDA(ctx, cudaGetLastError());
-    timing_end(ctx, "direct_luxels", ev);
-    return VRG_OK;
+    const DevScene s = scene_view(env);
+    const DevLight *lights = env->d_lights.as<DevLight>();
+    const int nl = (int)env->lights.size();
+    // variants: samples claimed per warp (32, 64, 128), picked per bucket
+    auto launch = [&](int v) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
+        if (e == cudaSuccess && d_rays) e = cudaMemsetAsync(d_rays, 0, 8, ctx->stream);
+        if (e != cudaSuccess) return e;
+        cudaEvent_t ev = nullptr;
+        timing_begin(ctx, "direct_luxels", &ev);
+        if (v == 0)
+            k_direct_luxels<32><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+        else if (v == 1)
+            k_direct_luxels<64><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+        else
+            k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+        e = cudaGetLastError();
+        timing_end(ctx, "direct_luxels", ev);
+        return e;
+    };
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss), 3, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

@@ -23,7 +23,7 @@ __device__ __forceinline__ void load3(const float *p, int64_t i, float &x, float
 // a device counter zeroed before the launch).  The occlusion bit goes into
 // the 1-bit mask with an atomic OR (the mask is zeroed before the launch).
 // WANT_HIT also writes the closest hit of the normalised segment.
-template <bool WANT_HIT>
+template <bool WANT_HIT, int LB>
 __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
                                                           int32_t skip, uint32_t *__restrict__ mask,
@@ -65,8 +65,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
         }
         if (active) {
             const bool done =
-                WANT_HIT ? trace_step<kClosest, 4>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
-                         : trace_step<kSkyOcc, 4>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
+                WANT_HIT ? trace_step<kClosest, LB>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
+                         : trace_step<kSkyOcc, LB>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
             if (done) {
                 active = false;
                 bool occ;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_closest(DevScene s, const fl
                 }
             }
         }
-        if (active && trace_step<kClosest, 4>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
+        if (active && trace_step<kClosest, 1>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
             active = false;
             hit[ri] = st.best;
             thit[ri] = st.best_t;
@@ -188,19 +188,30 @@ int launch_occlusion_mask(vrg_env *env, const float *start, const float *stop, i
     DevScene s = scene_view(env);
     VRG_CUDA(ctx, env->d_work.reserve(256));
     unsigned long long *work = env->d_work.as<unsigned long long>();
-    VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
-    VRG_CUDA(ctx, cudaMemsetAsync(mask, 0, 4 * (size_t)((n + 31) / 32), ctx->stream));
-    cudaEvent_t ev = nullptr;
-    timing_begin(ctx, "trace_mask", &ev);
-    if (hit && t)
-        k_trace_mask<true><<<persistent_grid(ctx, k_trace_mask<true>, n), kThreads, 0, ctx->stream>>>(
-            s, start, stop, n, skip_id, mask, hit, t, work);
-    else
-        k_trace_mask<false><<<persistent_grid(ctx, k_trace_mask<false>, n), kThreads, 0, ctx->stream>>>(
-            s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
-    VRG_CUDA(ctx, cudaGetLastError());
-    timing_end(ctx, "trace_mask", ev);
-    return VRG_OK;
+    const bool want = hit && t;
+    // variants: triangle planes fetched 1, 2 or 4 at a time (more overlap of
+    // loads against fewer resident warps); picked per scene-size bucket
+    auto launch = [&](int v) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(mask, 0, 4 * (size_t)((n + 31) / 32), ctx->stream);
+        if (e != cudaSuccess) return e;
+        cudaEvent_t ev = nullptr;
+        timing_begin(ctx, "trace_mask", &ev);
+        if (want) {
+            if (v == 0) k_trace_mask<true, 1><<<persistent_grid(ctx, k_trace_mask<true, 1>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t, work);
+            else if (v == 1) k_trace_mask<true, 2><<<persistent_grid(ctx, k_trace_mask<true, 2>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t, work);
+            else k_trace_mask<true, 4><<<persistent_grid(ctx, k_trace_mask<true, 4>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t, work);
+        } else {
+            if (v == 0) k_trace_mask<false, 1><<<persistent_grid(ctx, k_trace_mask<false, 1>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
+            else if (v == 1) k_trace_mask<false, 2><<<persistent_grid(ctx, k_trace_mask<false, 2>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
+            else k_trace_mask<false, 4><<<persistent_grid(ctx, k_trace_mask<false, 4>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
+        }
+        e = cudaGetLastError();
+        timing_end(ctx, "trace_mask", ev);
+        return e;
+    };
+    const std::string key = tune_key(want ? "trace_mask_hit" : "trace_mask", env->geom.ntris, n);
+    return tune_run(ctx, key, 3, launch);
 }
 
 int launch_trace_closest(vrg_env *env, const float *orig, const float *dir, const float *tmin,

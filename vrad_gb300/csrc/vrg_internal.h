@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -76,6 +77,9 @@ struct vrg_ctx {
     std::vector<vrg::PendingTiming> pending;
     std::vector<cudaEvent_t> event_pool;
     int64_t launches = 0;
+    bool autotune = true;
+    std::map<std::string, int> tuned;                   // bucket key -> variant
+    std::map<std::string, std::vector<double>> tune_ms;  // bucket key -> variant times
 };
 
 // Built kd tree + intersection records (host copy).
@@ -170,6 +174,11 @@ int cuda_fail(vrg_ctx *ctx, cudaError_t e, const char *what);
         cudaError_t _e = (call);                              \
         if (_e != cudaSuccess) return vrg::cuda_fail((ctx), _e, #call); \
     } while (0)
+
+// per-scene-size autotuning (tune.cpp)
+std::string tune_key(const char *kernel, int64_t scene_size, int64_t work);
+int tune_run(vrg_ctx *ctx, const std::string &key, int nvar,
+             const std::function<cudaError_t(int)> &launch);
 
 // timing around kernel launches
 void timing_begin(vrg_ctx *ctx, const char *name, cudaEvent_t *start);

@@ -85,6 +85,29 @@ class Context:
     def launch_count(self) -> int:
         return int(self.lib.vrg_ctx_launch_count(self.h))
 
+    def set_autotune(self, on: bool):
+        check(self.lib.vrg_ctx_set_autotune(self.h, int(on)), self.h, "set_autotune")
+
+    def autotune_choice(self, key: str):
+        """(variant, per-variant ms) of a tuned bucket; variant -1 if untuned."""
+        v = C.c_int32(-1)
+        ms = (C.c_double * 16)()
+        check(self.lib.vrg_ctx_autotune_choice(self.h, key.encode(), C.byref(v), ms, 16),
+              self.h, "autotune_choice")
+        return v.value, [x for x in ms if x > 0.0]
+
+    def autotune_save(self, path: str):
+        check(self.lib.vrg_ctx_autotune_save(self.h, str(path).encode()), self.h, "autotune_save")
+
+    def autotune_load(self, path: str):
+        check(self.lib.vrg_ctx_autotune_load(self.h, str(path).encode()), self.h, "autotune_load")
+
+    @staticmethod
+    def tune_key(site: str, triangles: int, work: int) -> str:
+        """Bucket key of a tuned launch site (floor log2 of both sizes)."""
+        lg = lambda v: int(v).bit_length() - 1 if v > 0 else 0
+        return f"{site}/t{lg(triangles)}/n{lg(work)}"
+
 
 def make_light(type_, origin, intensity, normal=(0.0, 0.0, -1.0), **keys) -> Light:
     """Builds one light the way CreateDirectLights does for an entity:
