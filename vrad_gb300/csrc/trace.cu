@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
                     p = plan_line(s, make_line(sx, sy, sz, ex, ey, ez));
                     active = !p.trivial && trace_init(s, p.ray, p.rp, p.slack, 0.0f, p.len, st);
                     if (!active && WANT_HIT) {
-                        hit[i] = -1;
-                        thit[i] = kInf;
+                        hit[ri] = -1;
+                        thit[ri] = kInf;
                     }
                 }
             }
@@ -80,6 +80,138 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
                 }
                 if (occ) atomicOr(mask + (ri >> 5), 1u << (ri & 31));
             }
+        }
+    }
+}
+
+// Shadow lines walked one unit of work per lane per round: each round every
+// busy lane either steps through one inner node or tests one triangle (a
+// lane that arrives at a leaf takes its triangle range and tests the first
+// one in the same round), so lanes at different depths and in leaves of
+// different sizes advance together instead of waiting for the slowest lane
+// of a descent or of a leaf (the "if-if" loop of Aila & Laine, HPG 2009).
+// Finished lanes take new lines when at least THRESH lanes are idle (or
+// none is busy), so the line setup runs for several lanes at once.  With
+// VOTE a round runs only the kind of unit (node step or triangle test) that
+// most lanes want, so the warp does not pay for both branches every round.
+// MINB is the resident-block hint of __launch_bounds__ (register cap).
+// Leaf order, pruning and tie rule are those of trace_step: same verdicts
+// and closest hits.
+template <bool WANT_HIT, int THRESH, bool VOTE, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const float *__restrict__ start,
+                                                          const float *__restrict__ stop, int64_t n,
+                                                          int32_t skip, uint32_t *__restrict__ mask,
+                                                          int32_t *__restrict__ hit,
+                                                          float *__restrict__ thit,
+                                                          unsigned long long *__restrict__ work) {
+    constexpr int MODE = WANT_HIT ? kClosest : kSkyOcc;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int64_t ri = 0;
+    Ray ray{};
+    RayPre rp{};
+    float len = 0.0f, any_limit = 0.0f;
+    uint32_t node = 0;
+    uint2 nd = make_uint2(0u, 0u);
+    float t0 = 0.0f, t1 = 0.0f;
+    int sp = 0;
+    uint32_t lpos = 0, lend = 0;  // triangles of the current leaf still to test
+    int32_t best = -1;
+    float best_t = kInf;
+    uint4 stk[kStackMax];
+    for (;;) {
+        const unsigned idle = __ballot_sync(full, !active && !exhausted);
+        const unsigned busy = __ballot_sync(full, active);
+        if (idle == 0 && busy == 0) break;
+        if (idle != 0 && (__popc(idle) >= THRESH || busy == 0)) {
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(full, base, leader);
+            if (!active && !exhausted) {
+                const int64_t i = (int64_t)base + __popc(idle & below);
+                if (i >= n) {
+                    exhausted = true;
+                } else {
+                    ri = i;
+                    float sx, sy, sz, ex, ey, ez;
+                    load3(start, i, sx, sy, sz);
+                    load3(stop, i, ex, ey, ez);
+                    const LinePlan p = plan_line(s, make_line(sx, sy, sz, ex, ey, ez));
+                    ray = p.ray;
+                    rp = p.rp;
+                    len = p.len;
+                    any_limit = p.any_limit;
+                    best = -1;
+                    best_t = kInf;
+                    sp = 0;
+                    lpos = lend = 0;
+                    t0 = 0.0f;
+                    t1 = p.len;
+                    bool go = !p.trivial && s.g.ntris > 0;
+                    if (go) {
+                        clip_box(s.g.bmin, s.g.bmax, p.slack, ray, rp, t0, t1);
+                        go = t0 <= t1;
+                    }
+                    if (go) {
+                        node = 0;
+                        nd = __ldg(&s.nodes[0]);
+                        active = true;
+                    } else if (WANT_HIT) {
+                        hit[ri] = -1;
+                        thit[ri] = kInf;
+                    }
+                }
+            }
+        }
+        bool done = false;
+        if (active && lpos == lend && (nd.x & 3u) == 3u) {
+            lpos = nd.x >> 2;
+            lend = lpos + (uint32_t)__uint_as_float(nd.y);
+            if (lpos == lend) {  // empty leaf
+                if (pop_next<MODE>(stk, sp, best_t, node, t0, t1))
+                    nd = __ldg(&s.nodes[node]);
+                else
+                    done = true;
+            }
+        }
+        // (a leaf popped after an empty one waits a round)
+        bool run_tri = active && !done && lpos < lend;
+        bool run_node = active && !done && lpos == lend && (nd.x & 3u) != 3u;
+        if (VOTE) {
+            const int ct = __popc(__ballot_sync(full, run_tri));
+            const int cn = __popc(__ballot_sync(full, run_node));
+            run_tri = run_tri && ct >= cn;
+            run_node = run_node && cn > ct;
+        }
+        if (run_tri) {
+            const float4 w0 = __ldg(s.leaf_planes + lpos);
+            if (tri_test<MODE>(s, ray, 0.0f, len, skip, any_limit, w0, lpos, best, best_t)) {
+                done = true;
+            } else if (++lpos == lend) {
+                if (pop_next<MODE>(stk, sp, best_t, node, t0, t1))
+                    nd = __ldg(&s.nodes[node]);
+                else
+                    done = true;
+            }
+        } else if (run_node) {
+            node = inner_step(rp, nd, t0, t1, stk, sp);
+            nd = __ldg(&s.nodes[node]);
+        }
+        if (done) {
+            active = false;
+            bool occ;
+            if (WANT_HIT) {
+                hit[ri] = best;
+                thit[ri] = best_t;
+                occ = best >= 0 && best_t < len && (__ldg(&s.tri_ids[best]) & kTraceIdSky) == 0;
+            } else {
+                occ = best >= 0 &&
+                      (best_t < any_limit || (__ldg(&s.tri_ids[best]) & kTraceIdSky) == 0);
+            }
+            if (occ) atomicOr(mask + (ri >> 5), 1u << (ri & 31));
         }
     }
 }
@@ -169,6 +301,24 @@ int persistent_grid(const vrg_ctx *ctx, K kernel, int64_t n) {
     return (int)(blocks < 1 ? 1 : blocks);
 }
 
+using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int32_t, uint32_t *,
+                            int32_t *, float *, unsigned long long *);
+
+// Variants of the shadow-line walk, picked per scene-size bucket: per-lane
+// refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
+// lanes, with or without the vote, at the default or a 40-register cap).
+const MaskKernel kMaskOcc[] = {
+    k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
+    k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
+    k_trace_unit<false, 4, false, 12>, k_trace_unit<false, 4, true, 12>,
+};
+const MaskKernel kMaskHit[] = {
+    k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
+    k_trace_unit<true, 4, true, 1>, k_trace_unit<true, 8, true, 1>,
+    k_trace_unit<true, 4, false, 12>, k_trace_unit<true, 4, true, 12>,
+};
+constexpr int kMaskVariants = 6;
+
 }  // namespace
 
 DevScene scene_view(const vrg_env *env) {
@@ -189,29 +339,25 @@ int launch_occlusion_mask(vrg_env *env, const float *start, const float *stop, i
     VRG_CUDA(ctx, env->d_work.reserve(256));
     unsigned long long *work = env->d_work.as<unsigned long long>();
     const bool want = hit && t;
-    // variants: triangle planes fetched 1, 2 or 4 at a time (more overlap of
-    // loads against fewer resident warps); picked per scene-size bucket
+    if (!want) {
+        hit = nullptr;
+        t = nullptr;
+    }
     auto launch = [&](int v) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(mask, 0, 4 * (size_t)((n + 31) / 32), ctx->stream);
         if (e != cudaSuccess) return e;
+        const MaskKernel k = want ? kMaskHit[v] : kMaskOcc[v];
         cudaEvent_t ev = nullptr;
         timing_begin(ctx, "trace_mask", &ev);
-        if (want) {
-            if (v == 0) k_trace_mask<true, 1><<<persistent_grid(ctx, k_trace_mask<true, 1>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t, work);
-            else if (v == 1) k_trace_mask<true, 2><<<persistent_grid(ctx, k_trace_mask<true, 2>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t, work);
-            else k_trace_mask<true, 4><<<persistent_grid(ctx, k_trace_mask<true, 4>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, hit, t, work);
-        } else {
-            if (v == 0) k_trace_mask<false, 1><<<persistent_grid(ctx, k_trace_mask<false, 1>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
-            else if (v == 1) k_trace_mask<false, 2><<<persistent_grid(ctx, k_trace_mask<false, 2>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
-            else k_trace_mask<false, 4><<<persistent_grid(ctx, k_trace_mask<false, 4>, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask, nullptr, nullptr, work);
-        }
+        k<<<persistent_grid(ctx, k, n), kThreads, 0, ctx->stream>>>(s, start, stop, n, skip_id, mask,
+                                                                     hit, t, work);
         e = cudaGetLastError();
         timing_end(ctx, "trace_mask", ev);
         return e;
     };
     const std::string key = tune_key(want ? "trace_mask_hit" : "trace_mask", env->geom.ntris, n);
-    return tune_run(ctx, key, 3, launch);
+    return tune_run(ctx, key, kMaskVariants, launch);
 }
 
 int launch_trace_closest(vrg_env *env, const float *orig, const float *dir, const float *tmin,

@@ -158,6 +158,7 @@ struct vrg_env {
     // scratch for host-buffer entry points
     vrg::DevBuf d_in0, d_in1, d_out0, d_out1, d_out2, d_counter;
     vrg::DevBuf d_work;  // work-queue counters of the persistent kernels
+    vrg::DevBuf d_bins;  // binned shadow lines (counts, points, order)
 
     // ray stream queue
     std::vector<float> rs_start, rs_stop;

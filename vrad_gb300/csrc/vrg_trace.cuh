@@ -111,8 +111,7 @@ struct TraceState {
     int sp;
     int32_t best;
     float best_t;
-    uint32_t st_node[kStackMax];
-    float st_t0[kStackMax], st_t1[kStackMax];
+    uint4 stk[kStackMax];  // (node, t0 bits, t1 bits, unused): one 16-byte access
 };
 
 // Starts a walk; returns false when the ray misses the scene's padded box
@@ -130,115 +129,148 @@ __device__ __forceinline__ bool trace_init(const DevScene &s, const Ray &ray, co
     return st.t0 <= st.t1;
 }
 
+// One step through an inner node: returns the child that holds the first
+// part of [t0, t1] and narrows the interval to it; the other child is pushed
+// (with its part of the interval) when the ray reaches it too.  The stack
+// never overflows: it holds at most one entry per tree level.
+__device__ __forceinline__ uint32_t inner_step(const RayPre &rp, uint2 nd, float &t0, float &t1,
+                                               uint4 *stk, int &sp) {
+    const uint32_t type = nd.x & 3u;
+    const float sv = __uint_as_float(nd.y);
+    const uint32_t left = nd.x >> 2;
+    const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
+    const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
+    const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
+    const uint32_t neg = (rp.neg >> type) & 1u;
+    const uint32_t nearc = left + neg, farc = left + 1u - neg;
+    const float tne = __fmaf_rn(sv, inv, A);
+    const float tfe = __fmaf_rn(sv, inv, B);
+    const bool vn = !(tne < t0), vf = !(tfe > t1);
+    if (vn) {
+        if (vf && sp < kStackMax) {
+            stk[sp] = make_uint4(farc, __float_as_uint(fmaxf(t0, tfe)), __float_as_uint(t1), 0u);
+            sp++;
+        }
+        t1 = fminf(t1, tne);
+        return nearc;
+    }
+    t0 = fmaxf(t0, tfe);
+    return farc;
+}
+
 // Ray/triangle test (project semantics, in this operation order):
 //   den = (Nx*dx + Ny*dy) + Nz*dz ; t = (D - ((Nx*ox + Ny*oy) + Nz*oz)) / den
 //   tmin <= t < tmax ; h = o + t*d on the two kept axes
 //   b0 = (e0*h0 + e1*h1) + e2 ; b1 = (e3*h0 + e4*h1) + e5 ; b2 = (1 - b0) - b1
 //   hit iff all three are >= 0.
+// Tests TriangleIndexList entry k, whose plane w0 the caller has loaded, and
+// updates best / best_t (minimum t, ties to the lower index).  Returns true
+// when the walk ends here: any accepted hit in kAny mode, a hit before
+// any_limit in kSkyOcc mode.  The edge part is fetched only when the plane
+// hit is in range.
+template <int MODE>
+__device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
+                                         int32_t skip, float any_limit, const float4 w0, size_t k,
+                                         int32_t &best, float &best_t) {
+    const float den = dot3r(w0.x, w0.y, w0.z, ray.dx, ray.dy, ray.dz);
+    const float on = dot3r(w0.x, w0.y, w0.z, ray.ox, ray.oy, ray.oz);
+    const float t = rdiv(rsub(w0.w, on), den);
+    if (!(t >= tmin && t < tmax)) return false;
+    if (MODE != kAny && !(t <= best_t)) return false;
+    const float4 *ed = s.leaf_edges + 2 * k;
+    const float4 w2 = __ldg(ed + 1);
+    if (__float_as_int(w2.z) == skip) return false;
+    const float4 w1 = __ldg(ed);
+    const uint32_t idx_drop = __float_as_uint(w2.w);
+    const int drop = (int)(idx_drop & 3u);
+    // kept axes (drop+1)%3, (drop+2)%3
+    const float o0 = drop == 0 ? ray.oy : (drop == 1 ? ray.oz : ray.ox);
+    const float o1 = drop == 0 ? ray.oz : (drop == 1 ? ray.ox : ray.oy);
+    const float d0 = drop == 0 ? ray.dy : (drop == 1 ? ray.dz : ray.dx);
+    const float d1 = drop == 0 ? ray.dz : (drop == 1 ? ray.dx : ray.dy);
+    const float h0 = radd(o0, rmul(t, d0));
+    const float h1 = radd(o1, rmul(t, d1));
+    const float b0 = radd(radd(rmul(w1.x, h0), rmul(w1.y, h1)), w1.z);
+    const float b1 = radd(radd(rmul(w1.w, h0), rmul(w2.x, h1)), w2.y);
+    const float b2 = rsub(rsub(1.0f, b0), b1);
+    if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
+        const int32_t ti = (int32_t)(idx_drop >> 2);
+        if (MODE == kAny || (MODE == kSkyOcc && t < any_limit)) {
+            best = ti;
+            best_t = t;
+            return true;
+        }
+        if (t < best_t || ti < best) {
+            best = ti;
+            best_t = t;
+        }
+    }
+    return false;
+}
+
+// Tests the cnt triangles of a leaf (TriangleIndexList[start .. start+cnt))
+// with tri_test; true when the walk ends here.  LB triangle planes are
+// fetched at a time so their loads overlap.
+template <int MODE, int LB>
+__device__ __forceinline__ bool leaf_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
+                                          int32_t skip, float any_limit, uint32_t start, int cnt,
+                                          int32_t &best, float &best_t) {
+    const float4 *pl = s.leaf_planes + start;
+    for (int k0 = 0; k0 < cnt; k0 += LB) {
+        float4 P[LB];
+#pragma unroll
+        for (int j = 0; j < LB; j++)
+            if (k0 + j < cnt) P[j] = __ldg(pl + k0 + j);
+#pragma unroll
+        for (int j = 0; j < LB; j++) {
+            if (k0 + j >= cnt) break;
+            if (tri_test<MODE>(s, ray, tmin, tmax, skip, any_limit, P[j], (size_t)start + k0 + j,
+                               best, best_t))
+                return true;
+        }
+    }
+    return false;
+}
+
+// Pops the next stacked subtree whose interval can still hold the answer
+// (kAny: every one); false when the stack is empty.
+template <int MODE>
+__device__ __forceinline__ bool pop_next(const uint4 *stk, int &sp, float best_t,
+                                         uint32_t &node, float &t0, float &t1) {
+    while (sp > 0) {
+        --sp;
+        const uint4 e = stk[sp];
+        if (MODE != kAny && __uint_as_float(e.y) > best_t) continue;
+        node = e.x;
+        t0 = __uint_as_float(e.y);
+        t1 = __uint_as_float(e.z);
+        return true;
+    }
+    return false;
+}
+
 // One step of the walk: descend to a leaf, test its triangles, pop the next
 // subtree that can still hold the answer.  Returns true when the walk is
-// over; the answer is st.best / st.best_t.  LB triangle planes are fetched
-// at a time so their loads overlap (more registers; latency-bound walks of
-// incoherent rays gain, register-capped gathers use 1).
+// over; the answer is st.best / st.best_t.
 template <int MODE, int LB = 1>
 __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, const RayPre &rp,
                                            float tmin, float tmax, int32_t skip, float any_limit,
                                            TraceState &st) {
-    const float ox = ray.ox, oy = ray.oy, oz = ray.oz, dx = ray.dx, dy = ray.dy, dz = ray.dz;
     uint32_t node = st.node;
     float t0 = st.t0, t1 = st.t1;
     int sp = st.sp;
     uint2 nd = __ldg(&s.nodes[node]);
-    uint32_t type = nd.x & 3u;
-    while (type != 3u) {
-        const float sv = __uint_as_float(nd.y);
-        const uint32_t left = nd.x >> 2;
-        const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
-        const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
-        const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
-        const uint32_t neg = (rp.neg >> type) & 1u;
-        const uint32_t nearc = left + neg, farc = left + 1u - neg;
-        const float tne = __fmaf_rn(sv, inv, A);
-        const float tfe = __fmaf_rn(sv, inv, B);
-        const bool vn = !(tne < t0), vf = !(tfe > t1);
-        if (vn) {
-            if (vf && sp < kStackMax) {
-                st.st_node[sp] = farc;
-                st.st_t0[sp] = fmaxf(t0, tfe);
-                st.st_t1[sp] = t1;
-                sp++;
-            }
-            node = nearc;
-            t1 = fminf(t1, tne);
-        } else {
-            node = farc;
-            t0 = fmaxf(t0, tfe);
-        }
+    while ((nd.x & 3u) != 3u) {
+        node = inner_step(rp, nd, t0, t1, st.stk, sp);
         nd = __ldg(&s.nodes[node]);
-        type = nd.x & 3u;
     }
-    // leaf: TriangleIndexList[start .. start+count)
-    const uint32_t start = nd.x >> 2;
-    const int cnt = (int)__uint_as_float(nd.y);
-    // planes are fetched LB at a time so their loads overlap; the edge part
-    // is fetched only for triangles whose plane hit is in range
-    constexpr int kLeafBatch = LB;
-    const float4 *pl = s.leaf_planes + start;
-    const float4 *ed = s.leaf_edges + 2 * (size_t)start;
-    for (int k0 = 0; k0 < cnt; k0 += kLeafBatch) {
-        float4 P[kLeafBatch];
-#pragma unroll
-        for (int j = 0; j < kLeafBatch; j++)
-            if (k0 + j < cnt) P[j] = __ldg(pl + k0 + j);
-#pragma unroll
-        for (int j = 0; j < kLeafBatch; j++) {
-        if (k0 + j >= cnt) break;
-        const float4 w0 = P[j];
-        const float den = dot3r(w0.x, w0.y, w0.z, dx, dy, dz);
-        const float on = dot3r(w0.x, w0.y, w0.z, ox, oy, oz);
-        const float t = rdiv(rsub(w0.w, on), den);
-        if (!(t >= tmin && t < tmax)) continue;
-        if (MODE != kAny && !(t <= st.best_t)) continue;
-        const float4 w2 = __ldg(ed + 2 * (k0 + j) + 1);
-        if (__float_as_int(w2.z) == skip) continue;
-        const float4 w1 = __ldg(ed + 2 * (k0 + j));
-        const uint32_t idx_drop = __float_as_uint(w2.w);
-        const int drop = (int)(idx_drop & 3u);
-        // kept axes (drop+1)%3, (drop+2)%3
-        const float o0 = drop == 0 ? oy : (drop == 1 ? oz : ox);
-        const float o1 = drop == 0 ? oz : (drop == 1 ? ox : oy);
-        const float d0 = drop == 0 ? dy : (drop == 1 ? dz : dx);
-        const float d1 = drop == 0 ? dz : (drop == 1 ? dx : dy);
-        const float h0 = radd(o0, rmul(t, d0));
-        const float h1 = radd(o1, rmul(t, d1));
-        const float b0 = radd(radd(rmul(w1.x, h0), rmul(w1.y, h1)), w1.z);
-        const float b1 = radd(radd(rmul(w1.w, h0), rmul(w2.x, h1)), w2.y);
-        const float b2 = rsub(rsub(1.0f, b0), b1);
-        if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
-            const int32_t ti = (int32_t)(idx_drop >> 2);
-            if (MODE == kAny || (MODE == kSkyOcc && t < any_limit)) {
-                st.best = ti;
-                st.best_t = t;
-                return true;
-            }
-            if (t < st.best_t || ti < st.best) {
-                st.best = ti;
-                st.best_t = t;
-            }
-        }
-        }
-    }
-    // next stacked subtree whose interval can still hold the answer
-    for (;;) {
-        if (sp == 0) return true;
-        --sp;
-        if (MODE != kAny && st.st_t0[sp] > st.best_t) continue;
-        st.node = st.st_node[sp];
-        st.t0 = st.st_t0[sp];
-        st.t1 = st.st_t1[sp];
-        st.sp = sp;
-        return false;
-    }
+    if (leaf_test<MODE, LB>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
+                            (int)__uint_as_float(nd.y), st.best, st.best_t))
+        return true;
+    if (!pop_next<MODE>(st.stk, sp, st.best_t, st.node, st.t0, st.t1))
+        return true;
+    st.sp = sp;
+    return false;
 }
 
 // A whole walk; returns the hit triangle index (-1 for none) and its t.
