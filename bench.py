@@ -401,6 +401,9 @@ def run_radiosity(args, local_rank):
     rows_ms = ctx.kernel_stats("transfer_rows")[0]
     gather_ms = ctx.kernel_stats("transfer_gather")[0]
     env.gather_patch_direct(nl)
+    env.bounce_light(nl, 100, 1e-3)  # the first solve of a size bucket tunes the SpMV
+    tkey = Context.tune_key("bounce_spmv", nnz, nl)
+    tv, tms = ctx.autotune_choice(tkey)
     # per-kernel timing pass (one launch per bounce)
     ctx.reset_stats()
     total, bounces, delta = env.bounce_light(nl, 100, 1e-3)
@@ -426,7 +429,9 @@ def run_radiosity(args, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 box rooms)",
         "config": {"workload": f"{lit.n_faces} faces subdivided at 64 units", "leaf_patches": nl,
                    "transfer_rays_per_patch": args.k, "nnz": nnz, "nnz_per_row": round(nnz / nl, 1),
-                   "bounces": bounces, "final_delta": delta},
+                   "bounces": bounces, "final_delta": delta,
+                   "autotune": {"bucket": tkey, "variant": tv,
+                                "variant_ms": [round(x, 4) for x in tms]}},
         "transfers": {"build_s": round(t_xfer, 3), "rows_kernel_ms": round(rows_ms, 3),
                       "gather_kernel_ms": round(gather_ms, 3),
                       "rays_per_s_M": round(nl * args.k / (rows_ms * 1e-3) / 1e6, 1),
@@ -627,7 +632,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the batch workload")
     ap.add_argument("--faces", type=int, default=4096,
                     help="lit faces of the direct-light scene (smaller only for profiling)")
-    ap.add_argument("--k", type=int, default=4096, help="transfer rays per patch (radiosity)")
+    ap.add_argument("--k", type=int, default=8192,
+                    help="transfer rays per patch (radiosity, batch, serve)")
     args = ap.parse_args()
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -639,13 +645,9 @@ def main():
             run_radiosity(args, local_rank)
     elif args.workload == "batch":
         if rank == 0:
-            if args.k == 4096:
-                args.k = 256
             run_batch(args, local_rank)
     elif args.workload == "serve":
         if rank == 0:
-            if args.k == 4096:
-                args.k = 256
             run_serve(args, local_rank)
     else:
         run_gpu(args, rank, world, local_rank)

@@ -17,6 +17,7 @@
 
 #include "vrg_gather.cuh"
 #include "vrg_internal.h"
+#include "vrg_spmv.cuh"
 
 namespace vrg {
 
@@ -175,30 +176,8 @@ __global__ void __launch_bounds__(kSpmvThreads) k_batch_spmv(const BatchDesc *__
         const float4 *emit_in = parity ? d->emit1 : d->emit0;
         float4 *emit_out = parity ? d->emit0 : d->emit1;
         const int64_t b = d->row_ptr[row], en = d->row_ptr[row + 1];
-        const int32_t *col = d->col;
-        const float *w = d->w;
-        float ar = 0.0f, ag = 0.0f, ab = 0.0f;
-        int64_t i = b + lane;
-        for (; i + 96 < en; i += 128) {
-            const int32_t c0 = __ldg(col + i), c1 = __ldg(col + i + 32), c2 = __ldg(col + i + 64), c3 = __ldg(col + i + 96);
-            const float w0 = __ldg(w + i), w1 = __ldg(w + i + 32), w2 = __ldg(w + i + 64), w3 = __ldg(w + i + 96);
-            const float4 e0 = __ldg(emit_in + c0), e1 = __ldg(emit_in + c1), e2 = __ldg(emit_in + c2), e3 = __ldg(emit_in + c3);
-            ar += w0 * e0.x + w1 * e1.x + w2 * e2.x + w3 * e3.x;
-            ag += w0 * e0.y + w1 * e1.y + w2 * e2.y + w3 * e3.y;
-            ab += w0 * e0.z + w1 * e1.z + w2 * e2.z + w3 * e3.z;
-        }
-        for (; i < en; i += 32) {
-            const float wv = __ldg(w + i);
-            const float4 ev = __ldg(emit_in + __ldg(col + i));
-            ar += wv * ev.x;
-            ag += wv * ev.y;
-            ab += wv * ev.z;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            ar += __shfl_xor_sync(0xffffffffu, ar, o);
-            ag += __shfl_xor_sync(0xffffffffu, ag, o);
-            ab += __shfl_xor_sync(0xffffffffu, ab, o);
-        }
+        const float3 a = warp_sum3(row_gather<4>(d->col, d->w, emit_in, b, en, lane));
+        const float ar = a.x, ag = a.y, ab = a.z;
         if (lane == 0) {
             float4 t = d->total[row];
             t.x += ar;

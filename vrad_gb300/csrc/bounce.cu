@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "vrg_internal.h"
+#include "vrg_spmv.cuh"
 
 namespace vrg {
 
@@ -50,8 +51,10 @@ __global__ void k_bounce_init(const LeafInfo *__restrict__ info, const float *__
     }
 }
 
-// One warp per row; lanes stride over the row's entries, then a butterfly
-// sum.  Per-block sums of |add| and |total| go to partials[2*block].
+// One warp per row (row_gather with U entries per lane per round), rows
+// strided over the grid's warps.  Per-block sums of |add| and |total| go to
+// partials[2*block].
+template <int U>
 __global__ void __launch_bounds__(kSpmvThreads) k_bounce_spmv(
     const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
     const float *__restrict__ w, const float4 *__restrict__ emit_in, float4 *__restrict__ emit_out,
@@ -63,38 +66,16 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bounce_spmv(
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double sa = 0.0, st = 0.0;
     for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nwarps) {
-        const int64_t b = row_ptr[row], e = row_ptr[row + 1];
-        float ar = 0.0f, ag = 0.0f, ab = 0.0f;
-        int64_t i = b + lane;
-        for (; i + 96 < e; i += 128) {
-            const int32_t c0 = __ldg(col + i), c1 = __ldg(col + i + 32), c2 = __ldg(col + i + 64), c3 = __ldg(col + i + 96);
-            const float w0 = __ldg(w + i), w1 = __ldg(w + i + 32), w2 = __ldg(w + i + 64), w3 = __ldg(w + i + 96);
-            const float4 e0 = __ldg(emit_in + c0), e1 = __ldg(emit_in + c1), e2 = __ldg(emit_in + c2), e3 = __ldg(emit_in + c3);
-            ar += w0 * e0.x + w1 * e1.x + w2 * e2.x + w3 * e3.x;
-            ag += w0 * e0.y + w1 * e1.y + w2 * e2.y + w3 * e3.y;
-            ab += w0 * e0.z + w1 * e1.z + w2 * e2.z + w3 * e3.z;
-        }
-        for (; i < e; i += 32) {
-            const float wv = __ldg(w + i);
-            const float4 ev = __ldg(emit_in + __ldg(col + i));
-            ar += wv * ev.x;
-            ag += wv * ev.y;
-            ab += wv * ev.z;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            ar += __shfl_xor_sync(0xffffffffu, ar, o);
-            ag += __shfl_xor_sync(0xffffffffu, ag, o);
-            ab += __shfl_xor_sync(0xffffffffu, ab, o);
-        }
+        const float3 a = warp_sum3(row_gather<U>(col, w, emit_in, row_ptr[row], row_ptr[row + 1], lane));
         if (lane == 0) {
             float4 t = total[row];
-            t.x += ar;
-            t.y += ag;
-            t.z += ab;
+            t.x += a.x;
+            t.y += a.y;
+            t.z += a.z;
             total[row] = t;
             const float4 r = info[row].refl;
-            emit_out[row] = make_float4(r.x * ar, r.y * ag, r.z * ab, 0.0f);
-            sa += (double)fabsf(ar) + (double)fabsf(ag) + (double)fabsf(ab);
+            emit_out[row] = make_float4(r.x * a.x, r.y * a.y, r.z * a.z, 0.0f);
+            sa += (double)fabsf(a.x) + (double)fabsf(a.y) + (double)fabsf(a.z);
             st += (double)fabsf(t.x) + (double)fabsf(t.y) + (double)fabsf(t.z);
         }
     }
@@ -148,28 +129,61 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
     const int64_t n = (int64_t)env->patches.leaf_patch.size();
     VRG_CUDA(ctx, env->d_emit.reserve(2 * 16 * (size_t)std::max<int64_t>(n, 1)));
     VRG_CUDA(ctx, env->d_total.reserve(16 * (size_t)std::max<int64_t>(n, 1)));
-    const int nblocks = ctx->num_sms * 4;
-    VRG_CUDA(ctx, env->d_partials.reserve(16 * (size_t)nblocks));
+    VRG_CUDA(ctx, env->d_partials.reserve(16 * (size_t)ctx->num_sms * 8));
     VRG_CUDA(ctx, env->d_control.reserve(sizeof(BounceControl)));
     float4 *e0 = env->d_emit.as<float4>(), *e1 = e0 + std::max<int64_t>(n, 1);
     BounceControl *ctl = env->d_control.as<BounceControl>();
     const int ib = (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), (int64_t)ctx->num_sms * 8);
-    cudaEvent_t ev = nullptr;
-    timing_begin(ctx, "bounce_init", &ev);
-    k_bounce_init<<<ib, 256, 0, ctx->stream>>>(env->d_leaf_info.as<LeafInfo>(), env->d_leaf_direct.as<float>(), e0,
-                                               env->d_total.as<float4>(), n, ctl, max_bounces, rel_tol);
-    VRG_CUDA(ctx, cudaGetLastError());
-    timing_end(ctx, "bounce_init", ev);
+    auto init = [&]() -> cudaError_t {
+        cudaEvent_t ev = nullptr;
+        timing_begin(ctx, "bounce_init", &ev);
+        k_bounce_init<<<ib, 256, 0, ctx->stream>>>(env->d_leaf_info.as<LeafInfo>(), env->d_leaf_direct.as<float>(),
+                                                   e0, env->d_total.as<float4>(), n, ctl, max_bounces, rel_tol);
+        cudaError_t e = cudaGetLastError();
+        timing_end(ctx, "bounce_init", ev);
+        return e;
+    };
+    VRG_CUDA(ctx, init());
 
-    auto one_bounce = [&](float4 *in, float4 *out) -> cudaError_t {
+    // SpMV variants, picked per (nnz, rows) bucket: 4, 8 or 2 entries per
+    // lane per round (the same sums).  Each runs one wave: resident blocks
+    // per SM times SMs.
+    using SpmvKernel = void (*)(const int64_t *, const int32_t *, const float *, const float4 *,
+                                float4 *, float4 *, const LeafInfo *, int64_t,
+                                const BounceControl *, double *);
+    const SpmvKernel kvar[3] = {k_bounce_spmv<4>, k_bounce_spmv<8>, k_bounce_spmv<2>};
+    auto spmv_blocks = [&](int v) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kvar[v], kSpmvThreads, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 2;
+        return ctx->num_sms * std::min(per_sm, 8);
+    };
+    auto spmv = [&](int v, float4 *in, float4 *out) -> cudaError_t {
         cudaEvent_t ev2 = nullptr;
         timing_begin(ctx, "bounce_spmv", &ev2);
-        k_bounce_spmv<<<nblocks, kSpmvThreads, 0, ctx->stream>>>(
+        const SpmvKernel k = kvar[v];
+        k<<<spmv_blocks(v), kSpmvThreads, 0, ctx->stream>>>(
             env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), in, out,
             env->d_total.as<float4>(), env->d_leaf_info.as<LeafInfo>(), n, ctl, env->d_partials.as<double>());
         cudaError_t e = cudaGetLastError();
         timing_end(ctx, "bounce_spmv", ev2);
+        return e;
+    };
+    int var = 0;
+    if (n > 0 && max_bounces > 0) {
+        bool ran = false;
+        const int rc = tune_pick(ctx, tune_key("bounce_spmv", env->nnz, n), 3,
+                                 [&](int v) { ran = true; return spmv(v, e0, e1); }, &var);
+        if (rc != VRG_OK) return rc;
+        if (ran) VRG_CUDA(ctx, init());  // tuning ran bounces: start over
+    }
+    const int nblocks = spmv_blocks(var);
+
+    auto one_bounce = [&](float4 *in, float4 *out) -> cudaError_t {
+        cudaError_t e = spmv(var, in, out);
         if (e != cudaSuccess) return e;
+        cudaEvent_t ev2 = nullptr;
         timing_begin(ctx, "bounce_reduce", &ev2);
         k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, env->d_partials.as<double>(), nblocks);
         e = cudaGetLastError();
@@ -328,7 +342,7 @@ extern "C" int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, f
     int32_t launched = 0;
     while (launched < max_bounces) {
         float4 *in = (launched & 1) ? e1 : e0, *out = (launched & 1) ? e0 : e1;
-        k_bounce_spmv<<<nblocks, kSpmvThreads, 0, ctx->stream>>>(
+        k_bounce_spmv<4><<<nblocks, kSpmvThreads, 0, ctx->stream>>>(
             env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), in, out, total,
             env->d_leaf_info.as<LeafInfo>(), n, ctl, partials);
         VRG_CUDA(ctx, cudaGetLastError());

@@ -29,6 +29,7 @@
 
 #include "vrg_gather.cuh"
 #include "vrg_internal.h"
+#include "vrg_spmv.cuh"
 
 namespace vrg {
 
@@ -190,20 +191,8 @@ __global__ void __launch_bounds__(kSpmvThreads) k_relight_spmv(
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double sd = 0.0, sy = 0.0;
     for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nwarps) {
-        const int64_t b = row_ptr[row], e = row_ptr[row + 1];
-        float ar = 0.0f, ag = 0.0f, ab = 0.0f;
-        for (int64_t i = b + lane; i < e; i += 32) {
-            const float wv = __ldg(w + i);
-            const float4 xv = __ldg(x_in + __ldg(col + i));
-            ar += wv * xv.x;
-            ag += wv * xv.y;
-            ab += wv * xv.z;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            ar += __shfl_xor_sync(0xffffffffu, ar, o);
-            ag += __shfl_xor_sync(0xffffffffu, ag, o);
-            ab += __shfl_xor_sync(0xffffffffu, ab, o);
-        }
+        const float3 a = warp_sum3(row_gather<4>(col, w, x_in, row_ptr[row], row_ptr[row + 1], lane));
+        const float ar = a.x, ag = a.y, ab = a.z;
         if (lane == 0) {
             const float4 old = B[row];
             B[row] = make_float4(ar, ag, ab, 0.0f);

@@ -6,7 +6,8 @@
 // in a scene-size bucket (log2 of the triangle count and of the work size)
 // runs every variant once on the real input, timed with CUDA events, and
 // keeps the fastest; later launches in that bucket use it directly.  Inside
-// a stream capture, or with tuning switched off, variant 0 runs.
+// a stream capture, or with tuning switched off, an untuned bucket runs
+// variant 0.
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -30,27 +31,20 @@ std::string tune_key(const char *kernel, int64_t scene_size, int64_t work) {
     return k.str();
 }
 
-int tune_run(vrg_ctx *ctx, const std::string &key, int nvar,
-             const std::function<cudaError_t(int)> &launch) {
-    int v = 0;
+int tune_pick(vrg_ctx *ctx, const std::string &key, int nvar,
+              const std::function<cudaError_t(int)> &launch, int *variant) {
+    *variant = 0;
     bool tune = false;
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
-        if (ctx->autotune) {
-            auto it = ctx->tuned.find(key);
-            if (it != ctx->tuned.end()) v = it->second;
-            else tune = true;
-        }
+        auto it = ctx->tuned.find(key);
+        if (it != ctx->tuned.end()) *variant = it->second < nvar ? it->second : 0;
+        else tune = ctx->autotune;
     }
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
-        if (tune) v = 0;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
         tune = false;
-    }
-    if (!tune || nvar < 2) {
-        VRG_CUDA(ctx, launch(v));
-        return VRG_OK;
-    }
+    if (!tune || nvar < 2) return VRG_OK;
     cudaEvent_t a = nullptr, b = nullptr;
     VRG_CUDA(ctx, cudaEventCreate(&a));
     VRG_CUDA(ctx, cudaEventCreate(&b));
@@ -74,6 +68,17 @@ int tune_run(vrg_ctx *ctx, const std::string &key, int nvar,
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->tuned[key] = best;
     ctx->tune_ms[key] = ms;
+    *variant = best;
+    return VRG_OK;
+}
+
+int tune_run(vrg_ctx *ctx, const std::string &key, int nvar,
+             const std::function<cudaError_t(int)> &launch) {
+    bool ran = false;
+    int v = 0;
+    const int rc = tune_pick(ctx, key, nvar, [&](int i) { ran = true; return launch(i); }, &v);
+    if (rc != VRG_OK || ran) return rc;  // a tuning run already produced the result
+    VRG_CUDA(ctx, launch(v));
     return VRG_OK;
 }
 

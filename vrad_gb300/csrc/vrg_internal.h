@@ -158,7 +158,6 @@ struct vrg_env {
     // scratch for host-buffer entry points
     vrg::DevBuf d_in0, d_in1, d_out0, d_out1, d_out2, d_counter;
     vrg::DevBuf d_work;  // work-queue counters of the persistent kernels
-    vrg::DevBuf d_bins;  // binned shadow lines (counts, points, order)
 
     // ray stream queue
     std::vector<float> rs_start, rs_stop;
@@ -176,8 +175,12 @@ int cuda_fail(vrg_ctx *ctx, cudaError_t e, const char *what);
         if (_e != cudaSuccess) return vrg::cuda_fail((ctx), _e, #call); \
     } while (0)
 
-// per-scene-size autotuning (tune.cpp)
+// per-scene-size autotuning (tune.cpp).  tune_pick returns the bucket's
+// variant, first timing every variant through `launch` when the bucket is
+// new; tune_run then launches the chosen one unless tuning just did.
 std::string tune_key(const char *kernel, int64_t scene_size, int64_t work);
+int tune_pick(vrg_ctx *ctx, const std::string &key, int nvar,
+              const std::function<cudaError_t(int)> &launch, int *variant);
 int tune_run(vrg_ctx *ctx, const std::string &key, int nvar,
              const std::function<cudaError_t(int)> &launch);
 
