@@ -232,6 +232,7 @@ void vrg_env_destroy(vrg_env *env) {
     }
     cudaSetDevice(env->ctx->device);
     cudaStreamSynchronize(env->ctx->stream);
+    relight_release(env);
     delete env;
 }
 
@@ -472,6 +473,7 @@ int vrg_light_parse_point(const vrg_light_keys *keys, vrg_light *light) {
 int vrg_env_set_lights(vrg_env *env, const vrg_light *lights, int32_t n) {
     if (!env || n < 0 || (n > 0 && !lights)) return VRG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(env->mu);
+    env->relight_ready = false;  // the relight caches belong to the old table
     for (int32_t i = 0; i < n; i++) {
         const vrg_light &l = lights[i];
         if (l.type < 0 || l.type > 5 || !finite3(l.origin) || !finite3(l.intensity))
@@ -493,6 +495,7 @@ int vrg_env_set_faces(vrg_env *env, int32_t nfaces, const float *corner, const f
     if (!env || nfaces < 0) return VRG_ERR_INVALID;
     if (nfaces > 0 && (!corner || !u || !v || !normal || !nu || !nv || !luxscale)) return VRG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(env->mu);
+    env->relight_ready = false;
     vrg_ctx *ctx = env->ctx;
     if (!env->built) return fail(ctx, VRG_ERR_STATE, "set faces after SetupAccelerationStructure");
     for (int32_t f = 0; f < nfaces; f++)
@@ -614,6 +617,7 @@ int vrg_env_make_patches(vrg_env *env, float max_chop, float min_chop, int64_t *
     if (!(max_chop > 0.0f) || !(min_chop > 0.0f)) return VRG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(env->mu);
     vrg_ctx *ctx = env->ctx;
+    env->relight_ready = false;
     TRY(make_rect_patches(*env, max_chop, min_chop, env->patches));
     const PatchSet &P = env->patches;
     const size_t n = P.face.size(), nl = P.leaf_patch.size();
@@ -684,6 +688,7 @@ int vrg_env_make_transfers(vrg_env *env, const float *dirs_local, int32_t k, int
     if (!dirs_local || k < 32 || k > 16384 || (k & (k - 1)) != 0)
         return fail(env->ctx, VRG_ERR_UNSUPPORTED, "transfer ray count must be a power of two in [32, 16384]");
     std::lock_guard<std::mutex> lk(env->mu);
+    env->relight_ready = false;
     TRY(run_make_transfers(env, dirs_local, k));
     if (out_nnz) *out_nnz = env->nnz;
     return VRG_OK;

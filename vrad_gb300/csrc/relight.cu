@@ -24,6 +24,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <new>
 #include <thread>
 
@@ -37,7 +38,7 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kSpmvThreads = 256;
-constexpr int kRelightBlocks = 256;  // SpMV grid of a relight (partials slots)
+constexpr int kRelightMaxBlocks = 2048;  // SpMV grid cap of a relight (partials slots)
 
 struct RelightCtl {
     int32_t done, iters, max_iters;
@@ -67,14 +68,18 @@ __device__ __forceinline__ int seg_of(const int64_t *__restrict__ off, int n, in
 
 // Gather over a work list: the luxels of listed faces (all faces when
 // list.faces is null), then their leaf points.  SKY = kSkyWrite stores the
-// sky multipliers, kSkyRead reuses them.
+// sky multipliers and the point/spot visibility bits (vis_words words per
+// sample or point), kSkyRead reuses them and traces only the lights flagged
+// in `edited`.
 template <int SKY>
 __global__ void __launch_bounds__(kThreads, 8) k_relight_gather(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ luxel_off, int nfaces, RelightList list, int ss, uint64_t seed,
     float *__restrict__ lux_out, const float *__restrict__ ppts, const float *__restrict__ pnrm,
     float *__restrict__ pout, float *__restrict__ sky_lux, float *__restrict__ sky_pts, int sky_slots,
-    unsigned long long *__restrict__ work, unsigned long long *__restrict__ ray_count) {
+    uint32_t *__restrict__ vis_lux, uint32_t *__restrict__ vis_pts, int vis_words,
+    const uint32_t *__restrict__ edited, unsigned long long *__restrict__ work,
+    unsigned long long *__restrict__ ray_count) {
     const bool all = list.faces == nullptr;
     const int nf = list.nfaces;
     // totals of the two segments (in "all" mode the leaf list is {0, leaves})
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_relight_gather(
             float px, py, pz;
             luxel_sample(fr, lux, iu, iv, kk, ss, seed, px, py, pz);
             gather_point<SKY>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g,
-                              b, rays, sky_lux + gsamp * sky_slots);
+                              b, rays, sky_lux + gsamp * sky_slots, vis_lux + gsamp * vis_words, edited);
         } else if (gi < total) {
             const int64_t li = gi - nsamp;
             int64_t leaf;
@@ -126,7 +131,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_relight_gather(
             }
             const float *p = ppts + 3 * leaf, *n = pnrm + 3 * leaf;
             gather_point<SKY>(s, lights, nl, __ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(n), __ldg(n + 1),
-                              __ldg(n + 2), r, g, b, rays, sky_pts + leaf * sky_slots);
+                              __ldg(n + 2), r, g, b, rays, sky_pts + leaf * sky_slots,
+                              vis_pts + leaf * vis_words, edited);
             pout[3 * leaf] = r;
             pout[3 * leaf + 1] = g;
             pout[3 * leaf + 2] = b;
@@ -218,8 +224,14 @@ __global__ void __launch_bounds__(kSpmvThreads) k_relight_spmv(
     }
 }
 
-__global__ void k_relight_reduce(RelightCtl *ctl, const double *__restrict__ partials, int nblocks) {
-    if (*(volatile int32_t *)&ctl->done) return;
+// Inside the loop graph (in_loop) thread 0 also sets the loop's condition:
+// the while node runs its body again only while the loop is not done.
+__global__ void k_relight_reduce(RelightCtl *ctl, const double *__restrict__ partials, int nblocks,
+                                 int in_loop, cudaGraphConditionalHandle loop) {
+    if (*(volatile int32_t *)&ctl->done) {
+        if (in_loop && threadIdx.x == 0) cudaGraphSetConditional(loop, 0u);
+        return;
+    }
     __shared__ double sa[256], st[256];
     double a = 0.0, t = 0.0;
     for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
@@ -240,7 +252,9 @@ __global__ void k_relight_reduce(RelightCtl *ctl, const double *__restrict__ par
         const float delta = st[0] > 0.0 ? (float)(sa[0] / st[0]) : 0.0f;
         ctl->last_delta = delta;
         ctl->iters += 1;
-        if (delta < ctl->tol || ctl->iters >= ctl->max_iters) ctl->done = 1;
+        const int done = delta < ctl->tol || ctl->iters >= ctl->max_iters;
+        if (done) ctl->done = 1;
+        if (in_loop) cudaGraphSetConditional(loop, done ? 0u : 1u);
     }
 }
 
@@ -284,6 +298,9 @@ __global__ void k_digest_final(const double *__restrict__ partials, int nblocks,
     }
 }
 
+// Words of the per-item visibility cache: one bit per light.
+int vis_words(size_t nlights) { return (int)((nlights + 31) / 32); }
+
 int count_sky(const std::vector<vrg_light> &lights) {
     int n = 0;
     for (const vrg_light &l : lights)
@@ -299,22 +316,35 @@ int persistent_blocks(vrg_ctx *ctx, const void *kernel, int64_t items) {
                                                        (int64_t)ctx->num_sms * per_sm));
 }
 
+int spmv_blocks(const vrg_ctx *ctx) {
+    static const int per_sm = [] {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_relight_spmv, kSpmvThreads, 0) != cudaSuccess || v < 1)
+            v = 2;
+        return v;
+    }();
+    return std::min(kRelightMaxBlocks, ctx->num_sms * per_sm);
+}
+
 }  // namespace
 
 // Per-slot device scratch of a relight request.
 struct RelightScratch {
-    DevBuf buf;  // [ctl | counters | digest | partials | face list | offsets]
-    size_t cap_faces = 0;
+    DevBuf buf;  // [ctl | counters | digest | partials | offsets | face list | edited mask]
+    size_t cap_faces = 0, cap_words = 0;
     RelightCtl *ctl = nullptr;
     unsigned long long *work = nullptr, *rays = nullptr;
     double *digest = nullptr, *partials = nullptr;
     int32_t *faces = nullptr, *leaf_beg = nullptr;
     int64_t *samp_off = nullptr, *leaf_off = nullptr;
+    uint32_t *edited = nullptr;
 
-    int reserve(vrg_ctx *ctx, size_t nfaces) {
-        if (nfaces <= cap_faces && buf.ptr) return VRG_OK;
-        const size_t head = 256 + 2 * 8 * kRelightBlocks;
-        const size_t bytes = head + (nfaces + 1) * (4 + 4 + 8 + 8) + 256;
+    int reserve(vrg_ctx *ctx, size_t nfaces, size_t nwords) {
+        if (nfaces <= cap_faces && nwords <= cap_words && buf.ptr) return VRG_OK;
+        nfaces = std::max(nfaces, cap_faces);
+        nwords = std::max(nwords, cap_words);
+        const size_t head = 256 + 2 * 8 * kRelightMaxBlocks;
+        const size_t bytes = head + (nfaces + 1) * (4 + 4 + 8 + 8) + 4 * nwords + 256;
         VRG_CUDA(ctx, buf.reserve(bytes));
         char *p = buf.as<char>();
         ctl = reinterpret_cast<RelightCtl *>(p);
@@ -327,11 +357,58 @@ struct RelightScratch {
         leaf_off = samp_off + (nfaces + 1);
         faces = reinterpret_cast<int32_t *>(leaf_off + (nfaces + 1));
         leaf_beg = faces + (nfaces + 1);
+        edited = reinterpret_cast<uint32_t *>(leaf_beg + (nfaces + 1));
         cap_faces = nfaces;
+        cap_words = nwords;
         return VRG_OK;
     }
 };
 
+struct HostStage {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    ~HostStage() {
+        if (ptr) cudaFreeHost(ptr);
+    }
+    int reserve(vrg_ctx *ctx, size_t n) {
+        if (n <= bytes && ptr) return VRG_OK;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        VRG_CUDA(ctx, cudaMallocHost(&ptr, n));
+        bytes = n;
+        return VRG_OK;
+    }
+};
+
+// The warm-start bounce loop of one (scene, scratch) pair as an executable
+// graph: a while node whose body is SpMV x0 -> x1, reduce, SpMV x1 -> x0,
+// reduce.  The reduce kernels clear the loop condition once the control
+// block is done, so the loop stops on the device after the last useful
+// iteration instead of running no-op launches up to the cap.
+struct LoopGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void *> key;  // the buffers and sizes it was built on
+    LoopGraph() = default;
+    LoopGraph(const LoopGraph &) = delete;
+    LoopGraph &operator=(const LoopGraph &) = delete;
+    ~LoopGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+// Relight state a scene keeps between requests: the serial entry point's
+// scratch and staging buffer, and the loop graphs built for each scratch.
+struct RelightState {
+    RelightScratch sc;
+    HostStage stage;
+    std::map<const RelightScratch *, std::unique_ptr<LoopGraph>> loops;
+};
+
+void relight_release(vrg_env *env) {
+    delete env->relight;
+    env->relight = nullptr;
+}
 }  // namespace vrg
 
 using namespace vrg;
@@ -349,16 +426,20 @@ int relight_prepare(vrg_env *env, int32_t ss, uint64_t seed, int32_t max_bounces
     const int64_t nlux = env->luxel_offset.back();
     const int64_t nl = (int64_t)env->patches.leaf_patch.size();
     const int sky = count_sky(env->lights);
-    const size_t need = 12 * (size_t)nlux + 4 * (size_t)(nlux * ss + nl) * std::max(sky, 1) + 16 * 4 * (size_t)nl +
-                        12 * (size_t)nl;
+    const int vw = vis_words(env->lights.size());
+    const size_t need = 12 * (size_t)nlux + 4 * (size_t)(nlux * ss + nl) * (std::max(sky, 1) + vw) +
+                        16 * 4 * (size_t)nl + 12 * (size_t)nl;
     size_t free_b = 0, total_b = 0;
     VRG_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
     if (need + ((size_t)1 << 30) > free_b)
         return fail(ctx, VRG_ERR_NOMEM, "not enough free device memory to admit this scene for relighting");
+    relight_release(env);  // loop graphs point into buffers that may move below
     VRG_CUDA(ctx, env->d_bake_rgb.reserve(12 * (size_t)std::max<int64_t>(nlux, 1)));
     VRG_CUDA(ctx, env->d_leaf_direct.reserve(12 * (size_t)std::max<int64_t>(nl, 1)));
     VRG_CUDA(ctx, env->d_sky_lux.reserve(4 * (size_t)std::max<int64_t>(nlux * ss * sky, 1)));
     VRG_CUDA(ctx, env->d_sky_pts.reserve(4 * (size_t)std::max<int64_t>(nl * sky, 1)));
+    VRG_CUDA(ctx, env->d_vis_lux.reserve(4 * (size_t)std::max<int64_t>(nlux * ss * vw, 1)));
+    VRG_CUDA(ctx, env->d_vis_pts.reserve(4 * (size_t)std::max<int64_t>(nl * vw, 1)));
     VRG_CUDA(ctx, env->d_emit0.reserve(16 * (size_t)std::max<int64_t>(nl, 1)));
     VRG_CUDA(ctx, env->d_x.reserve(2 * 16 * (size_t)std::max<int64_t>(nl, 1)));
     VRG_CUDA(ctx, env->d_work.reserve(256));
@@ -391,6 +472,8 @@ int relight_prepare(vrg_env *env, int32_t ss, uint64_t seed, int32_t max_bounces
     cudaStream_t st = ctx->stream;
     unsigned long long *work = env->d_work.as<unsigned long long>() + 4;
     VRG_CUDA(ctx, cudaMemsetAsync(work, 0, 8, st));
+    VRG_CUDA(ctx, cudaMemsetAsync(env->d_vis_lux.ptr, 0, 4 * (size_t)(nlux * ss * vw), st));
+    VRG_CUDA(ctx, cudaMemsetAsync(env->d_vis_pts.ptr, 0, 4 * (size_t)(nl * vw), st));
     RelightList all{};
     // leaf_off of the "all" list: {0, nl} from a tiny device array
     int64_t off2[2] = {0, nl};
@@ -407,7 +490,8 @@ int relight_prepare(vrg_env *env, int32_t ss, uint64_t seed, int32_t max_bounces
         scene_view(env), env->d_lights.as<DevLight>(), (int)env->lights.size(), env->d_faces.as<FaceRec>(),
         env->d_luxel_offset.as<int64_t>(), env->nfaces, all, ss, seed, env->d_bake_rgb.as<float>(),
         env->d_patch_pts.as<float>(), env->d_patch_nrm.as<float>(), env->d_leaf_direct.as<float>(),
-        env->d_sky_lux.as<float>(), env->d_sky_pts.as<float>(), sky, work, nullptr);
+        env->d_sky_lux.as<float>(), env->d_sky_pts.as<float>(), sky, env->d_vis_lux.as<uint32_t>(),
+        env->d_vis_pts.as<uint32_t>(), vw, nullptr, work, nullptr);
     VRG_CUDA(ctx, cudaGetLastError());
     timing_end(ctx, "relight_gather", ev);
     env->have_patch_direct = true;
@@ -417,6 +501,7 @@ int relight_prepare(vrg_env *env, int32_t ss, uint64_t seed, int32_t max_bounces
     if (rc != VRG_OK) return rc;
     VRG_CUDA(ctx, cudaStreamSynchronize(st));
     env->sky_slots = sky;
+    env->vis_words = vw;
     env->relight_ss = ss;
     env->relight_seed = seed;
     env->relight_ready = true;
@@ -442,6 +527,7 @@ bool sphere_hits_box(const float *c, float radius, const float *lo, const float 
 
 struct RelightPlan {
     std::vector<vrg_light> table;  // new light table
+    std::vector<uint32_t> edited;  // bit k: light k changed (its shadow lines are re-traced)
     std::vector<int32_t> faces;    // affected faces (empty + all=true: every face)
     bool all = false;
     bool any = false;
@@ -452,6 +538,7 @@ struct RelightPlan {
 int plan_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, RelightPlan &p) {
     vrg_ctx *ctx = env->ctx;
     p.table = env->lights;
+    p.edited.assign((size_t)vis_words(p.table.size()), 0u);
     std::vector<std::pair<vrg_light, vrg_light>> changed;
     for (int32_t i = 0; i < n; i++) {
         const int32_t k = edits[i].index;
@@ -467,7 +554,10 @@ int plan_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, RelightPl
                 return fail(ctx, VRG_ERR_UNSUPPORTED, "relight can change a sky light's intensity only");
         }
         if (nw.type < 0 || nw.type > 5) return fail(ctx, VRG_ERR_INVALID, "bad light type in edit");
-        if (!light_equal(old, nw)) changed.emplace_back(old, nw);
+        if (!light_equal(old, nw)) {
+            changed.emplace_back(old, nw);
+            p.edited[k >> 5] |= 1u << (k & 31);
+        }
         p.table[k] = nw;
     }
     p.any = !changed.empty();
@@ -494,22 +584,65 @@ int plan_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, RelightPl
     return VRG_OK;
 }
 
-struct HostStage {
-    void *ptr = nullptr;
-    size_t bytes = 0;
-    ~HostStage() {
-        if (ptr) cudaFreeHost(ptr);
-    }
-    int reserve(vrg_ctx *ctx, size_t n) {
-        if (n <= bytes && ptr) return VRG_OK;
-        if (ptr) cudaFreeHost(ptr);
-        ptr = nullptr;
-        bytes = 0;
-        VRG_CUDA(ctx, cudaMallocHost(&ptr, n));
-        bytes = n;
+RelightState &relight_state(vrg_env *env) {
+    if (!env->relight) env->relight = new RelightState;
+    return *env->relight;
+}
+
+// The loop graph of (env, sc), built on first use and rebuilt when a buffer
+// it points into has moved.
+int loop_graph(vrg_env *env, RelightScratch &sc, cudaStream_t st, int sblocks, cudaGraphExec_t *out) {
+    vrg_ctx *ctx = env->ctx;
+    const int64_t n = (int64_t)env->patches.leaf_patch.size();
+    float4 *B = env->d_total.as<float4>(), *emit = env->d_emit0.as<float4>();
+    float4 *x0 = env->d_x.as<float4>(), *x1 = x0 + std::max<int64_t>(n, 1);
+    const std::vector<const void *> key = {x0, B, emit, env->d_row_ptr.ptr, env->d_col.ptr, env->d_weight.ptr,
+                                           env->d_leaf_info.ptr, sc.ctl, sc.partials,
+                                           reinterpret_cast<const void *>((intptr_t)n),
+                                           reinterpret_cast<const void *>((intptr_t)sblocks)};
+    std::unique_ptr<LoopGraph> &slot = relight_state(env).loops[&sc];
+    if (slot && slot->key == key) {
+        *out = slot->exec;
         return VRG_OK;
     }
-};
+    slot.reset(new LoopGraph);
+    cudaGraph_t g = nullptr;
+    VRG_CUDA(ctx, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h = 0;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wn = nullptr;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&wn, g, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const LeafInfo *info = env->d_leaf_info.as<LeafInfo>();
+        const int64_t *rp = env->d_row_ptr.as<int64_t>();
+        const int32_t *col = env->d_col.as<int32_t>();
+        const float *w = env->d_weight.as<float>();
+        k_relight_spmv<<<sblocks, kSpmvThreads, 0, st>>>(rp, col, w, x0, x1, B, emit, info, n, sc.ctl, sc.partials);
+        k_relight_reduce<<<1, 256, 0, st>>>(sc.ctl, sc.partials, sblocks, 1, h);
+        k_relight_spmv<<<sblocks, kSpmvThreads, 0, st>>>(rp, col, w, x1, x0, B, emit, info, n, sc.ctl, sc.partials);
+        k_relight_reduce<<<1, 256, 0, st>>>(sc.ctl, sc.partials, sblocks, 1, h);
+        const cudaError_t le = cudaGetLastError();
+        cudaGraph_t captured = nullptr;
+        e = cudaStreamEndCapture(st, &captured);
+        if (e == cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&slot->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        slot.reset();
+        return cuda_fail(ctx, e, "relight loop graph");
+    }
+    slot->key = key;
+    *out = slot->exec;
+    return VRG_OK;
+}
 
 // Issues one relight on `st`: table upload, partial re-gather, warm bounce,
 // digest.  Nothing here waits on the GPU.
@@ -518,18 +651,21 @@ int issue_relight(vrg_env *env, const RelightPlan &p, int32_t max_iters, float t
     vrg_ctx *ctx = env->ctx;
     const int32_t F = env->nfaces;
     const int32_t nf = p.all ? F : (int32_t)p.faces.size();
-    int rc = sc.reserve(ctx, (size_t)std::max(nf, 1));
+    int rc = sc.reserve(ctx, (size_t)std::max(nf, 1), p.edited.size());
     if (rc != VRG_OK) return rc;
     // host staging: light table, then the face list and offsets
     const size_t lbytes = 80 * p.table.size();
+    const size_t ebytes = 4 * p.edited.size();
     const size_t fbytes = (size_t)(nf + 1) * (8 + 8 + 4 + 4);
-    rc = stage.reserve(ctx, lbytes + fbytes + 64);
+    rc = stage.reserve(ctx, lbytes + ebytes + fbytes + 64);
     if (rc != VRG_OK) return rc;
     std::vector<float4> packed;
     pack_lights(p.table, packed);
     char *h = static_cast<char *>(stage.ptr);
     memcpy(h, packed.data(), lbytes);
-    int64_t *hs = reinterpret_cast<int64_t *>(h + lbytes);
+    uint32_t *he = reinterpret_cast<uint32_t *>(h + lbytes);
+    memcpy(he, p.edited.data(), ebytes);
+    int64_t *hs = reinterpret_cast<int64_t *>(h + ((lbytes + ebytes + 7) & ~(size_t)7));
     int64_t *hl = hs + (nf + 1);
     int32_t *hf = reinterpret_cast<int32_t *>(hl + (nf + 1));
     int32_t *hb = hf + (nf + 1);
@@ -543,6 +679,7 @@ int issue_relight(vrg_env *env, const RelightPlan &p, int32_t max_iters, float t
         hl[k + 1] = hl[k] + (env->face_leaf_begin[2 * f + 1] - env->face_leaf_begin[2 * f]);
     }
     VRG_CUDA(ctx, cudaMemcpyAsync(env->d_lights.ptr, h, lbytes, cudaMemcpyHostToDevice, st));
+    VRG_CUDA(ctx, cudaMemcpyAsync(sc.edited, he, ebytes, cudaMemcpyHostToDevice, st));
     VRG_CUDA(ctx, cudaMemcpyAsync(sc.samp_off, hs, 8 * (size_t)(nf + 1), cudaMemcpyHostToDevice, st));
     VRG_CUDA(ctx, cudaMemcpyAsync(sc.leaf_off, hl, 8 * (size_t)(nf + 1), cudaMemcpyHostToDevice, st));
     VRG_CUDA(ctx, cudaMemcpyAsync(sc.faces, hf, 4 * (size_t)(nf + 1), cudaMemcpyHostToDevice, st));
@@ -555,7 +692,9 @@ int issue_relight(vrg_env *env, const RelightPlan &p, int32_t max_iters, float t
             scene_view(env), env->d_lights.as<DevLight>(), (int)p.table.size(), env->d_faces.as<FaceRec>(),
             env->d_luxel_offset.as<int64_t>(), F, list, ss, env->relight_seed, env->d_bake_rgb.as<float>(),
             env->d_patch_pts.as<float>(), env->d_patch_nrm.as<float>(), env->d_leaf_direct.as<float>(),
-            env->d_sky_lux.as<float>(), env->d_sky_pts.as<float>(), env->sky_slots, sc.work, sc.rays);
+            env->d_sky_lux.as<float>(), env->d_sky_pts.as<float>(), env->sky_slots,
+            env->d_vis_lux.as<uint32_t>(), env->d_vis_pts.as<uint32_t>(), env->vis_words, sc.edited, sc.work,
+            sc.rays);
         VRG_CUDA(ctx, cudaGetLastError());
     }
     const int64_t n = (int64_t)env->patches.leaf_patch.size();
@@ -565,20 +704,18 @@ int issue_relight(vrg_env *env, const RelightPlan &p, int32_t max_iters, float t
     k_relight_start<<<ib, 256, 0, st>>>(env->d_leaf_info.as<LeafInfo>(), env->d_leaf_direct.as<float>(), B, emit,
                                         x0, n, sc.ctl, max_iters, tol);
     VRG_CUDA(ctx, cudaGetLastError());
-    for (int32_t it = 0; it < max_iters; it++) {
-        k_relight_spmv<<<kRelightBlocks, kSpmvThreads, 0, st>>>(
-            env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), (it & 1) ? x1 : x0,
-            (it & 1) ? x0 : x1, B, emit, env->d_leaf_info.as<LeafInfo>(), n, sc.ctl, sc.partials);
-        k_relight_reduce<<<1, 256, 0, st>>>(sc.ctl, sc.partials, kRelightBlocks);
-    }
-    VRG_CUDA(ctx, cudaGetLastError());
+    // the loop runs on the device until the control block is done
+    cudaGraphExec_t loop = nullptr;
+    rc = loop_graph(env, sc, st, spmv_blocks(ctx), &loop);
+    if (rc != VRG_OK) return rc;
+    VRG_CUDA(ctx, cudaGraphLaunch(loop, st));
     k_digest_partial<<<kDigestBlocks, 256, 0, st>>>(env->d_bake_rgb.as<float>(), 3 * env->luxel_offset.back(), B, n,
                                                      sc.partials);
     k_digest_final<<<1, 32, 0, st>>>(sc.partials, kDigestBlocks, sc.digest);
     VRG_CUDA(ctx, cudaGetLastError());
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
-        ctx->launches += 4 + 2 * (int64_t)max_iters + (items > 0 ? 1 : 0);
+        ctx->launches += 3 + (items > 0 ? 1 : 0);  // plus the loop graph's kernels
     }
     return VRG_OK;
 }
@@ -650,6 +787,7 @@ void finish_slot(vrg_server *s, Slot &sl) {
 
 int start_slot(vrg_server *s, Slot &sl, Request *r) {
     vrg_env *env = s->scenes[r->scene];
+    std::lock_guard<std::mutex> lk(env->mu);  // the scene's tables and relight state
     RelightPlan plan;
     int rc = plan_relight(env, r->edits.data(), (int32_t)r->edits.size(), plan);
     if (rc != VRG_OK) return rc;
@@ -722,9 +860,9 @@ int vrg_env_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, int32_
     RelightPlan plan;
     int rc = plan_relight(env, edits, n, plan);
     if (rc != VRG_OK) return rc;
-    RelightScratch sc;
-    HostStage stage;
-    rc = issue_relight(env, plan, max_iters, rel_tol, ctx->stream, sc, stage);
+    RelightState &rs = relight_state(env);
+    RelightScratch &sc = rs.sc;
+    rc = issue_relight(env, plan, max_iters, rel_tol, ctx->stream, sc, rs.stage);
     if (rc != VRG_OK) return rc;
     env->lights = plan.table;
     RelightCtl c;

@@ -44,16 +44,21 @@ __device__ __forceinline__ uint64_t splitmix(uint64_t seed, uint64_t i) {
 // which do not depend on any light position: 0 traces them; 1 traces them
 // and stores each one's multiplier (cosine or visible fraction, -1 when it
 // adds nothing) in sky[0..]; 2 reads those multipliers instead of tracing.
-// The accumulation order and arithmetic are the same in all three, so a
-// relight that re-traces only point and spot lights is bit-identical to a
-// full gather.
+// With a visibility cache vis (one bit per light, bit li of word li/32),
+// mode 1 also stores whether each traced point/spot shadow line reached its
+// light, and mode 2 traces only the lights flagged in `edited` (refreshing
+// their bits) and takes every other light's visibility from the cache.
+// The accumulation order and arithmetic are the same in all modes, so a
+// relight that re-traces only edited lights is bit-identical to a full
+// gather with the edited table.
 enum SkyMode { kSkyTrace = 0, kSkyWrite = 1, kSkyRead = 2 };
 
 template <int SKY>
 static __device__ void gather_point(const DevScene &s, const DevLight *__restrict__ lights, int nl,
                                     float px, float py, float pz, float nx, float ny, float nz,
                                     float &r, float &g, float &b, uint32_t &rays,
-                                    float *__restrict__ sky = nullptr) {
+                                    float *__restrict__ sky = nullptr, uint32_t *__restrict__ vis = nullptr,
+                                    const uint32_t *__restrict__ edited = nullptr) {
     float ar = 0.0f, ag = 0.0f, ab = 0.0f;
     for (int li = 0; li < nl; li++) {
         const float4 lo = __ldg(&lights[li].origin);
@@ -94,8 +99,19 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
                 if (ln.w == 1.0f) f = rmul(f, dot2);
                 else if (ln.w != 0.0f) f = rmul(f, powf(dot2, ln.w));
             }
-            rays++;
-            if (line_occluded(s, make_line(px, py, pz, lo.x, lo.y, lo.z), -1)) continue;
+            bool occ;
+            const uint32_t bit = 1u << (li & 31);
+            if (SKY == kSkyRead && vis && !(__ldg(edited + (li >> 5)) & bit)) {
+                occ = !(vis[li >> 5] & bit);
+            } else {
+                rays++;
+                occ = line_occluded(s, make_line(px, py, pz, lo.x, lo.y, lo.z), -1);
+                if (SKY != kSkyTrace && vis) {
+                    if (occ) vis[li >> 5] &= ~bit;
+                    else vis[li >> 5] |= bit;
+                }
+            }
+            if (occ) continue;
             const float sc = rmul(f, cosr);
             ar = radd(ar, rmul(li_i.x, sc));
             ag = radd(ag, rmul(li_i.y, sc));

@@ -52,6 +52,8 @@ struct DevBuf {
     template <class T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+struct RelightState;  // relight.cu: serial scratch and loop graphs of a scene
+
 struct KernelStat {
     double ms = 0.0;
     int64_t launches = 0;
@@ -151,7 +153,10 @@ struct vrg_env {
     int32_t relight_ss = 4;
     uint64_t relight_seed = 0;
     int32_t sky_slots = 0;
+    int32_t vis_words = 0;                  // visibility-cache words per sample / point
     vrg::DevBuf d_sky_lux, d_sky_pts, d_emit0, d_x;
+    vrg::DevBuf d_vis_lux, d_vis_pts;       // point/spot shadow-line bits per sample / point
+    vrg::RelightState *relight = nullptr;   // owned; freed by relight_release
     std::vector<float> face_lo, face_hi;      // face bounds (3 floats each)
     std::vector<int32_t> face_leaf_begin;     // leaves of face f: [begin[f], begin[f+1])
 
@@ -215,5 +220,6 @@ void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst);
 int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k);
 int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounces,
                float *delta);
+void relight_release(vrg_env *env);
 
 }  // namespace vrg
