@@ -195,6 +195,8 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.set_stream(stream)
     lib_ctx = Context(local_rank)
     lib_ctx.set_stream(stream.cuda_stream)
+    if args.autotune_file:
+        lib_ctx.autotune_load(args.autotune_file)
     lib = lib_ctx.lib
 
     if args.workload == "anyhit":
@@ -382,6 +384,8 @@ def run_radiosity(args, local_rank):
 
     torch.cuda.set_device(local_rank)
     ctx = Context(local_rank)
+    if args.autotune_file:
+        ctx.autotune_load(args.autotune_file)
     lit = scenes.lit_scene(SEED, n_faces=args.faces)
     env = Environment(ctx)
     env.add_triangles(lit.xyz, lit.ids)
@@ -632,6 +636,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the batch workload")
     ap.add_argument("--faces", type=int, default=4096,
                     help="lit faces of the direct-light scene (smaller only for profiling)")
+    ap.add_argument("--autotune-file", default=None,
+                    help="load saved autotune choices ('bucket variant' lines) before running")
     ap.add_argument("--k", type=int, default=8192,
                     help="transfer rays per patch (radiosity, batch, serve)")
     args = ap.parse_args()

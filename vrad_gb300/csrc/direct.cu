@@ -23,7 +23,7 @@ constexpr int kThreads = 128;
 // Persistent warps take FETCH samples at a time from work[0] (zeroed before
 // the launch), so faces with many occluders do not leave SMs idle; larger
 // claims mean fewer atomics, smaller ones a shorter tail.
-template <int FETCH>
+template <int FETCH, bool STREAM = false>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             const int iv = (int)(local / fr.nu), iu = (int)(local - (int64_t)iv * fr.nu);
             float px, py, pz;
             luxel_sample(fr, lux, iu, iv, k, ss, seed, px, py, pz);
-            gather_point<kSkyTrace>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g, b, rays);
+            gather_point<kSkyTrace, STREAM>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g,
+                                            b, rays);
         }
         if (ss == 4) {
             const float r1 = __shfl_down_sync(0xffffffffu, r, 1), r2 = __shfl_down_sync(0xffffffffu, r, 2), r3 = __shfl_down_sync(0xffffffffu, r, 3);
@@ -139,7 +140,8 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     const DevScene s = scene_view(env);
     const DevLight *lights = env->d_lights.as<DevLight>();
     const int nl = (int)env->lights.size();
-    // variants: samples claimed per warp (32, 64, 128), picked per bucket
+    // variants: samples claimed per warp (32, 64, 128), and 32 with the leaf
+    // records kept out of L1; picked per bucket
     auto launch = [&](int v) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
         if (e == cudaSuccess && d_rays) e = cudaMemsetAsync(d_rays, 0, 8, ctx->stream);
@@ -150,13 +152,15 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
             k_direct_luxels<32><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
         else if (v == 1)
             k_direct_luxels<64><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
-        else
+        else if (v == 2)
             k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+        else
+            k_direct_luxels<32, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss), 3, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss), 4, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

@@ -23,7 +23,7 @@ __device__ __forceinline__ void load3(const float *p, int64_t i, float &x, float
 // a device counter zeroed before the launch).  The occlusion bit goes into
 // the 1-bit mask with an atomic OR (the mask is zeroed before the launch).
 // WANT_HIT also writes the closest hit of the normalised segment.
-template <bool WANT_HIT, int LB>
+template <bool WANT_HIT, int LB, bool STREAM = false>
 __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
                                                           int32_t skip, uint32_t *__restrict__ mask,
@@ -65,8 +65,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
         }
         if (active) {
             const bool done =
-                WANT_HIT ? trace_step<kClosest, LB>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
-                         : trace_step<kSkyOcc, LB>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
+                WANT_HIT ? trace_step<kClosest, LB, STREAM>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
+                         : trace_step<kSkyOcc, LB, STREAM>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
             if (done) {
                 active = false;
                 bool occ;
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
 // MINB is the resident-block hint of __launch_bounds__ (register cap).
 // Leaf order, pruning and tie rule are those of trace_step: same verdicts
 // and closest hits.
-template <bool WANT_HIT, int THRESH, bool VOTE, int MINB>
+template <bool WANT_HIT, int THRESH, bool VOTE, int MINB, bool STREAM = false>
 __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
                                                           int32_t skip, uint32_t *__restrict__ mask,
@@ -187,8 +187,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
             run_node = run_node && cn > ct;
         }
         if (run_tri) {
-            const float4 w0 = __ldg(s.leaf_planes + lpos);
-            if (tri_test<MODE>(s, ray, 0.0f, len, skip, any_limit, w0, lpos, best, best_t)) {
+            const float4 w0 = leaf_load<STREAM>(s.leaf_planes + lpos);
+            if (tri_test<MODE, STREAM>(s, ray, 0.0f, len, skip, any_limit, w0, lpos, best, best_t)) {
                 done = true;
             } else if (++lpos == lend) {
                 if (pop_next<MODE>(stk, sp, best_t, node, t0, t1))
@@ -306,18 +306,23 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 
 // Variants of the shadow-line walk, picked per scene-size bucket: per-lane
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
-// lanes, with or without the vote, at the default or a 40-register cap).
+// lanes, with or without the vote, at the default or a 40-register cap,
+// leaf records kept out of L1 or not).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
     k_trace_unit<false, 4, false, 12>, k_trace_unit<false, 4, true, 12>,
+    k_trace_unit<false, 4, false, 1, true>, k_trace_unit<false, 8, false, 1, true>,
+    k_trace_mask<false, 1, true>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
     k_trace_unit<true, 4, true, 1>, k_trace_unit<true, 8, true, 1>,
     k_trace_unit<true, 4, false, 12>, k_trace_unit<true, 4, true, 12>,
+    k_trace_unit<true, 4, false, 1, true>, k_trace_unit<true, 8, false, 1, true>,
+    k_trace_mask<true, 1, true>,
 };
-constexpr int kMaskVariants = 6;
+constexpr int kMaskVariants = 9;
 
 }  // namespace
 

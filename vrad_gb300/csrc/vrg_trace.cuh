@@ -168,7 +168,20 @@ __device__ __forceinline__ uint32_t inner_step(const RayPre &rp, uint2 nd, float
 // when the walk ends here: any accepted hit in kAny mode, a hit before
 // any_limit in kSkyOcc mode.  The edge part is fetched only when the plane
 // hit is in range.
-template <int MODE>
+// Leaf-record load; STREAM asks L1 not to keep the line (the leaf records
+// of a large scene stream past L1, where they would evict the nodes and the
+// traversal stacks that are reused).
+template <bool STREAM>
+__device__ __forceinline__ float4 leaf_load(const float4 *p) {
+    if (!STREAM) return __ldg(p);
+    float4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+template <int MODE, bool STREAM = false>
 __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
                                          int32_t skip, float any_limit, const float4 w0, size_t k,
                                          int32_t &best, float &best_t) {
@@ -178,9 +191,9 @@ __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, floa
     if (!(t >= tmin && t < tmax)) return false;
     if (MODE != kAny && !(t <= best_t)) return false;
     const float4 *ed = s.leaf_edges + 2 * k;
-    const float4 w2 = __ldg(ed + 1);
+    const float4 w2 = leaf_load<STREAM>(ed + 1);
     if (__float_as_int(w2.z) == skip) return false;
-    const float4 w1 = __ldg(ed);
+    const float4 w1 = leaf_load<STREAM>(ed);
     const uint32_t idx_drop = __float_as_uint(w2.w);
     const int drop = (int)(idx_drop & 3u);
     // kept axes (drop+1)%3, (drop+2)%3
@@ -211,7 +224,7 @@ __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, floa
 // Tests the cnt triangles of a leaf (TriangleIndexList[start .. start+cnt))
 // with tri_test; true when the walk ends here.  LB triangle planes are
 // fetched at a time so their loads overlap.
-template <int MODE, int LB>
+template <int MODE, int LB, bool STREAM = false>
 __device__ __forceinline__ bool leaf_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
                                           int32_t skip, float any_limit, uint32_t start, int cnt,
                                           int32_t &best, float &best_t) {
@@ -220,12 +233,12 @@ __device__ __forceinline__ bool leaf_test(const DevScene &s, const Ray &ray, flo
         float4 P[LB];
 #pragma unroll
         for (int j = 0; j < LB; j++)
-            if (k0 + j < cnt) P[j] = __ldg(pl + k0 + j);
+            if (k0 + j < cnt) P[j] = leaf_load<STREAM>(pl + k0 + j);
 #pragma unroll
         for (int j = 0; j < LB; j++) {
             if (k0 + j >= cnt) break;
-            if (tri_test<MODE>(s, ray, tmin, tmax, skip, any_limit, P[j], (size_t)start + k0 + j,
-                               best, best_t))
+            if (tri_test<MODE, STREAM>(s, ray, tmin, tmax, skip, any_limit, P[j], (size_t)start + k0 + j,
+                                       best, best_t))
                 return true;
         }
     }
@@ -252,7 +265,7 @@ __device__ __forceinline__ bool pop_next(const uint4 *stk, int &sp, float best_t
 // One step of the walk: descend to a leaf, test its triangles, pop the next
 // subtree that can still hold the answer.  Returns true when the walk is
 // over; the answer is st.best / st.best_t.
-template <int MODE, int LB = 1>
+template <int MODE, int LB = 1, bool STREAM = false>
 __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, const RayPre &rp,
                                            float tmin, float tmax, int32_t skip, float any_limit,
                                            TraceState &st) {
@@ -264,7 +277,7 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
         node = inner_step(rp, nd, t0, t1, st.stk, sp);
         nd = __ldg(&s.nodes[node]);
     }
-    if (leaf_test<MODE, LB>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
+    if (leaf_test<MODE, LB, STREAM>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
                             (int)__uint_as_float(nd.y), st.best, st.best_t))
         return true;
     if (!pop_next<MODE>(st.stk, sp, st.best_t, st.node, st.t0, st.t1))
@@ -274,12 +287,12 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
 }
 
 // A whole walk; returns the hit triangle index (-1 for none) and its t.
-template <int MODE>
+template <int MODE, bool STREAM = false>
 __device__ int32_t kd_trace(const DevScene &s, const Ray &ray, const RayPre &rp, float slack,
                             float tmin, float tmax, int32_t skip, float any_limit, float *t_out) {
     TraceState st;
     if (trace_init(s, ray, rp, slack, tmin, tmax, st))
-        while (!trace_step<MODE>(s, ray, rp, tmin, tmax, skip, any_limit, st)) {
+        while (!trace_step<MODE, 1, STREAM>(s, ray, rp, tmin, tmax, skip, any_limit, st)) {
         }
     *t_out = st.best_t;
     return st.best;
@@ -352,12 +365,13 @@ __device__ __forceinline__ bool line_verdict(const DevScene &s, const LinePlan &
     return (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
 }
 
+template <bool STREAM = false>
 __device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
     const LinePlan p = plan_line(s, L);
     if (p.trivial) return false;
     float th;
     const int32_t h =
-        kd_trace<kSkyOcc>(s, p.ray, p.rp, p.slack, 0.0f, p.len, skip, p.any_limit, &th);
+        kd_trace<kSkyOcc, STREAM>(s, p.ray, p.rp, p.slack, 0.0f, p.len, skip, p.any_limit, &th);
     return line_verdict(s, p, h, th);
 }
 
