@@ -336,7 +336,14 @@ def run_gpu(args, rank, world, local_rank):
                "kind": "port",
                "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
     achieved = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
-    traffic = _ncu_traffic(f"ncu_{kernel}.txt")
+    tkey = (Context.tune_key("trace_mask", env.num_triangles(), n) if args.workload == "anyhit"
+            else Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
+    tv, tms = lib_ctx.autotune_choice(tkey)
+    # DRAM traffic per launch from the committed ncu capture of the variant family in use
+    prof = f"ncu_{kernel}.txt"
+    if args.workload == "anyhit" and tv in (6, 7):
+        prof = "ncu_trace_unit_stream.txt"
+    traffic = _ncu_traffic(prof)
     torch.cuda.synchronize()
     l2 = _l2_read_gbs(local_rank)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -346,10 +353,7 @@ def run_gpu(args, rank, world, local_rank):
             "bytes_per_ray": round(bytes_per_unit, 2),
             "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
             "l2_read_gbs_measured": round(l2, 1) if l2 else None,
-            "l2_frac": round(achieved / l2, 4) if l2 else None}
-    tkey = (Context.tune_key("trace_mask", env.num_triangles(), n) if args.workload == "anyhit"
-            else Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
-    tv, tms = lib_ctx.autotune_choice(tkey)
+            "l2_frac": round(achieved / l2, 4) if l2 else None, "traffic_source": f"profiles/{prof}"}
     line = {
         "metric": "shadow Mrays/s (direct-light gather)" if args.workload != "anyhit"
         else "shadow Mrays/s (any-hit occlusion mask)",
