@@ -407,6 +407,7 @@ def run_radiosity(args, local_rank):
     nnz = env.make_transfers(dirs)
     t_xfer = time.perf_counter() - t0
     rows_ms = ctx.kernel_stats("transfer_rows")[0]
+    xkey = Context.tune_key("transfer_rows", env.num_triangles(), nl * args.k)
     gather_ms = ctx.kernel_stats("transfer_gather")[0]
     env.gather_patch_direct(nl)
     env.bounce_light(nl, 100, 1e-3)  # the first solve of a size bucket tunes the SpMV
@@ -443,6 +444,8 @@ def run_radiosity(args, local_rank):
         "transfers": {"build_s": round(t_xfer, 3), "rows_kernel_ms": round(rows_ms, 3),
                       "gather_kernel_ms": round(gather_ms, 3),
                       "rays_per_s_M": round(nl * args.k / (rows_ms * 1e-3) / 1e6, 1),
+                      "autotune": dict(zip(("bucket", "variant", "variant_ms"),
+                                           (xkey,) + ctx.autotune_choice(xkey))),
                       "patch_build_s": round(t_patch, 3)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,

@@ -17,11 +17,12 @@ namespace vrg {
 
 namespace {
 
-constexpr int kRowThreads = 256;
-
 // One block per row: trace the k rays, sort the k target ids in shared
-// memory (bitonic), then a block scan compacts runs into (col, count).
-__global__ void __launch_bounds__(kRowThreads) k_transfer_rows(
+// memory (bitonic), then a block scan compacts runs into (col, count).  NT
+// threads per block (at most k); STREAM loads the leaf records without
+// allocating in L1.
+template <int NT, bool STREAM>
+__global__ void __launch_bounds__(NT) k_transfer_rows(
     DevScene s, const LeafInfo *__restrict__ leaves, const FaceRec *__restrict__ faces,
     const PatchNode *__restrict__ pnodes, const int32_t *__restrict__ face_root,
     const int32_t *__restrict__ tri_face, const float *__restrict__ dirs, int k, int64_t row0,
@@ -30,7 +31,7 @@ __global__ void __launch_bounds__(kRowThreads) k_transfer_rows(
     extern __shared__ int32_t sm[];
     int32_t *tg = sm;         // k target ids
     int32_t *starts = sm + k; // k run starts
-    __shared__ int32_t warp_sums[kRowThreads / 32];
+    __shared__ int32_t warp_sums[NT / 32];
     __shared__ int32_t total_sh;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int64_t rl = blockIdx.x; rl < rows; rl += gridDim.x) {
@@ -53,7 +54,8 @@ __global__ void __launch_bounds__(kRowThreads) k_transfer_rows(
             const float dy = radd(radd(rmul(lx, t1y), rmul(ly, t2y)), rmul(lz, ny));
             const float dz = radd(radd(rmul(lx, t1z), rmul(ly, t2z)), rmul(lz, nz));
             float t;
-            const int32_t h = trace_ray<kClosest>(s, Ray{qx, qy, qz, dx, dy, dz}, 0.0f, kMaxTraceLength, -1, &t);
+            const int32_t h =
+                trace_ray<kClosest, STREAM>(s, Ray{qx, qy, qz, dx, dy, dz}, 0.0f, kMaxTraceLength, -1, &t);
             int32_t target = -1;
             if (h >= 0) {
                 const int32_t g = __ldg(tri_face + h);
@@ -174,12 +176,51 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k) {
     env->have_transfers = false;
     env->nnz = 0;
     env->transfer_k = k;
+    // The rays of a row go out in table order, one per lane.  A row's CSR
+    // does not depend on that order (hits are counted per target), so the
+    // table is put in 2-D Morton order of its (x, y) disk coordinates: then
+    // the 32 rays of a warp leave in neighbouring directions and walk much
+    // the same nodes, where the given lattice order sends them all over the
+    // hemisphere.
+    std::vector<float> dirs(dirs_local, dirs_local + 3 * (size_t)k);
+    {
+        auto spread = [](uint32_t v) {
+            v &= 0xffffu;
+            v = (v | (v << 8)) & 0x00ff00ffu;
+            v = (v | (v << 4)) & 0x0f0f0f0fu;
+            v = (v | (v << 2)) & 0x33333333u;
+            v = (v | (v << 1)) & 0x55555555u;
+            return v;
+        };
+        auto q = [](float c) {
+            const float u = (c + 1.0f) * 0.5f * 65535.0f;
+            return (uint32_t)(u < 0.0f ? 0.0f : (u > 65535.0f ? 65535.0f : u));
+        };
+        std::vector<std::pair<uint32_t, int32_t>> key(k);
+        for (int32_t r = 0; r < k; r++)
+            key[r] = {spread(q(dirs_local[3 * r])) | (spread(q(dirs_local[3 * r + 1])) << 1), r};
+        std::stable_sort(key.begin(), key.end(),
+                         [](const std::pair<uint32_t, int32_t> &a, const std::pair<uint32_t, int32_t> &b) {
+                             return a.first < b.first;
+                         });
+        for (int32_t r = 0; r < k; r++)
+            for (int c = 0; c < 3; c++) dirs[3 * r + c] = dirs_local[3 * key[r].second + c];
+    }
     DevBuf d_dirs;
     VRG_CUDA(ctx, d_dirs.reserve(12 * (size_t)k));
-    VRG_CUDA(ctx, cudaMemcpyAsync(d_dirs.ptr, dirs_local, 12 * (size_t)k, cudaMemcpyHostToDevice, ctx->stream));
-    const int threads = std::min(kRowThreads, k);
+    VRG_CUDA(ctx, cudaMemcpyAsync(d_dirs.ptr, dirs.data(), 12 * (size_t)k, cudaMemcpyHostToDevice, ctx->stream));
+    VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // `dirs` is pageable and goes out of scope
     const size_t smem = 2 * (size_t)k * sizeof(int32_t);
-    VRG_CUDA(ctx, cudaFuncSetAttribute(k_transfer_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // variants, picked per (triangles, rows) bucket: 256 or 512 threads per
+    // row block, leaf records through L1 or not
+    using RowKernel = void (*)(DevScene, const LeafInfo *, const FaceRec *, const PatchNode *, const int32_t *,
+                               const int32_t *, const float *, int, int64_t, int64_t, int32_t *, int32_t *,
+                               int32_t *);
+    const RowKernel kvar[4] = {k_transfer_rows<256, false>, k_transfer_rows<512, false>,
+                               k_transfer_rows<256, true>, k_transfer_rows<512, true>};
+    const int vthreads[4] = {256, 512, 256, 512};
+    for (int v = 0; v < 4; v++)
+        VRG_CUDA(ctx, cudaFuncSetAttribute(kvar[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // rows go through in chunks whose staging stays near 1 GiB
     const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(rows, ((int64_t)1 << 30) / (8 * (int64_t)k)));
     DevBuf stage_col, stage_cnt, d_nnz, d_rowptr_chunk;
@@ -194,13 +235,20 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k) {
         const int64_t nr = std::min(chunk, rows - r0);
         const int grid = (int)std::min<int64_t>(nr, (int64_t)ctx->num_sms * 8);
         cudaEvent_t ev = nullptr;
-        timing_begin(ctx, "transfer_rows", &ev);
-        k_transfer_rows<<<grid, threads, smem, ctx->stream>>>(
-            s, env->d_leaf_info.as<LeafInfo>(), env->d_faces.as<FaceRec>(), env->d_patch_nodes.as<PatchNode>(),
-            env->d_face_root.as<int32_t>(), env->d_tri_face.as<int32_t>(), d_dirs.as<float>(), k, r0, nr,
-            stage_col.as<int32_t>(), stage_cnt.as<int32_t>(), d_nnz.as<int32_t>());
-        VRG_CUDA(ctx, cudaGetLastError());
-        timing_end(ctx, "transfer_rows", ev);
+        auto launch = [&](int v) -> cudaError_t {
+            timing_begin(ctx, "transfer_rows", &ev);
+            const int threads = std::min(vthreads[v], k);
+            kvar[threads == vthreads[v] ? v : (v & 2)]<<<grid, threads, smem, ctx->stream>>>(
+                s, env->d_leaf_info.as<LeafInfo>(), env->d_faces.as<FaceRec>(),
+                env->d_patch_nodes.as<PatchNode>(), env->d_face_root.as<int32_t>(), env->d_tri_face.as<int32_t>(),
+                d_dirs.as<float>(), k, r0, nr, stage_col.as<int32_t>(), stage_cnt.as<int32_t>(),
+                d_nnz.as<int32_t>());
+            const cudaError_t e = cudaGetLastError();
+            timing_end(ctx, "transfer_rows", ev);
+            return e;
+        };
+        const int rc = tune_run(ctx, tune_key("transfer_rows", env->geom.ntris, rows * (int64_t)k), 4, launch);
+        if (rc != VRG_OK) return rc;
         VRG_CUDA(ctx, cudaMemcpyAsync(h_nnz.data(), d_nnz.ptr, 4 * (size_t)nr, cudaMemcpyDeviceToHost, ctx->stream));
         VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         for (int64_t i = 0; i < nr; i++) row_ptr[r0 + i + 1] = row_ptr[r0 + i] + h_nnz[i];

@@ -299,12 +299,12 @@ __device__ int32_t kd_trace(const DevScene &s, const Ray &ray, const RayPre &rp,
 }
 
 // Closest or first hit of one ray with its own setup.
-template <int MODE>
+template <int MODE, bool STREAM = false>
 __device__ __forceinline__ int32_t trace_ray(const DevScene &s, const Ray &ray, float tmin,
                                              float tmax, int32_t skip, float *t_out) {
     const float slack = ray_slack(s.g, ray.ox, ray.oy, ray.oz);
     const RayPre rp = ray_pre(ray, slack);
-    return kd_trace<MODE>(s, ray, rp, slack, tmin, tmax, skip, 0.0f, t_out);
+    return kd_trace<MODE, STREAM>(s, ray, rp, slack, tmin, tmax, skip, 0.0f, t_out);
 }
 
 // Shadow-line setup of TestLineDoesHitSky (raytracer/trace/testline.go:22-27):
