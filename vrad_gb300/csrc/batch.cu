@@ -463,11 +463,11 @@ int vrg_env_bake(vrg_env *env, int32_t supersamples, uint64_t seed, int32_t max_
         cnt = env->d_counter.as<unsigned long long>();
         VRG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, ctx->stream));
     }
-    rc = launch_gather_luxels(env, supersamples, seed, env->d_bake_rgb.as<float>(), cnt);
-    if (rc != VRG_OK) return rc;
+    // luxel samples and leaf-patch points in one persistent launch
     const int64_t nl = (int64_t)env->patches.leaf_patch.size();
-    rc = launch_gather_points(env, env->d_patch_pts.as<float>(), env->d_patch_nrm.as<float>(), nl,
-                              env->d_leaf_direct.as<float>(), cnt);
+    rc = launch_gather_luxels(env, supersamples, seed, env->d_bake_rgb.as<float>(), cnt,
+                              env->d_patch_pts.as<float>(), env->d_patch_nrm.as<float>(), nl,
+                              env->d_leaf_direct.as<float>());
     if (rc != VRG_OK) return rc;
     env->have_patch_direct = true;
     int32_t bounces = 0;

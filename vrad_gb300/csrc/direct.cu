@@ -23,27 +23,40 @@ constexpr int kThreads = 128;
 // Persistent warps take FETCH samples at a time from work[0] (zeroed before
 // the launch), so faces with many occluders do not leave SMs idle; larger
 // claims mean fewer atomics, smaller ones a shorter tail.
+// Optional second segment: npts sample points (pts, nrm: 3 floats each)
+// after the luxel samples, written to pout -- the leaf-patch points of a
+// bake, which alone are too few to fill the GPU.
 template <int FETCH, bool STREAM = false>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
-    float *__restrict__ out, unsigned long long *__restrict__ ray_count,
+    float *__restrict__ out, const float *__restrict__ pts, const float *__restrict__ nrm, int64_t npts,
+    float *__restrict__ pout, unsigned long long *__restrict__ ray_count,
     unsigned long long *__restrict__ work) {
     const int64_t nsamp = nlux * ss;
+    const int64_t total = nsamp + npts;
     const int lane = threadIdx.x & 31;
     uint32_t rays = 0;
     for (;;) {
         unsigned long long wb0 = 0;
         if (lane == 0) wb0 = atomicAdd(work, (unsigned long long)FETCH);
         wb0 = __shfl_sync(0xffffffffu, wb0, 0);
-        if (wb0 >= (unsigned long long)nsamp) break;
+        if (wb0 >= (unsigned long long)total) break;
         for (int sub = 0; sub < FETCH; sub += 32) {
         const unsigned long long wb = wb0 + sub;
-        if (wb >= (unsigned long long)nsamp) break;
+        if (wb >= (unsigned long long)total) break;
         const int64_t gi = (int64_t)wb + lane;
         float r = 0.0f, g = 0.0f, b = 0.0f;
         int64_t lux = 0;
-        if (gi < nsamp) {
+        if (gi >= nsamp && gi < total) {
+            const int64_t i = gi - nsamp;
+            gather_point<kSkyTrace, STREAM>(s, lights, nl, __ldg(pts + 3 * i), __ldg(pts + 3 * i + 1),
+                                            __ldg(pts + 3 * i + 2), __ldg(nrm + 3 * i), __ldg(nrm + 3 * i + 1),
+                                            __ldg(nrm + 3 * i + 2), r, g, b, rays);
+            pout[3 * i] = r;
+            pout[3 * i + 1] = g;
+            pout[3 * i + 2] = b;
+        } else if (gi < nsamp) {
             lux = gi / ss;
             const int k = (int)(gi - lux * ss);
             const int f = find_face(off, nfaces, lux);
@@ -125,17 +138,18 @@ void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst) {
 }
 
 int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
-                         unsigned long long *d_rays) {
+                         unsigned long long *d_rays, const float *pts, const float *nrm, int64_t npts,
+                         float *pts_out) {
     vrg_ctx *ctx = env->ctx;
     const int64_t nlux = env->luxel_offset.empty() ? 0 : env->luxel_offset.back();
-    if (nlux == 0) return VRG_OK;
+    if (nlux == 0 && npts == 0) return VRG_OK;
     VRG_CUDA(ctx, env->d_work.reserve(256));
     unsigned long long *work = env->d_work.as<unsigned long long>() + 1;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_luxels<32>, kThreads, 0) != cudaSuccess ||
         per_sm < 1)
         per_sm = 4;
-    const int64_t need = (nlux * ss + kThreads - 1) / kThreads;
+    const int64_t need = (nlux * ss + npts + kThreads - 1) / kThreads;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * per_sm));
     const DevScene s = scene_view(env);
     const DevLight *lights = env->d_lights.as<DevLight>();
@@ -149,18 +163,18 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
         cudaEvent_t ev = nullptr;
         timing_begin(ctx, "direct_luxels", &ev);
         if (v == 0)
-            k_direct_luxels<32><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+            k_direct_luxels<32><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else if (v == 1)
-            k_direct_luxels<64><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+            k_direct_luxels<64><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else if (v == 2)
-            k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+            k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else
-            k_direct_luxels<32, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, d_rays, work);
+            k_direct_luxels<32, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss), 4, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 4, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

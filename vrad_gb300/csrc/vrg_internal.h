@@ -212,8 +212,11 @@ int launch_trace_closest(vrg_env *env, const float *orig, const float *dir, cons
                          const float *tmax, int64_t n, int32_t skip_id, int32_t *hit, float *t);
 int launch_test_lines(vrg_env *env, const float *start, const float *stop, int64_t n,
                       int32_t skip_id, float *frac);
+// Luxel samples of every face, then (optionally) npts extra sample points
+// in the same persistent launch.
 int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
-                         unsigned long long *d_rays);
+                         unsigned long long *d_rays, const float *pts = nullptr,
+                         const float *nrm = nullptr, int64_t npts = 0, float *pts_out = nullptr);
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,
                          float *out_rgb, unsigned long long *d_rays);
 void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst);
