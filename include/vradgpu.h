@@ -96,18 +96,20 @@ int vrg_ctx_synchronize(vrg_ctx *ctx);
 /* Per-kernel CUDA-event timing of every launch (off by default). */
 int vrg_ctx_set_timing(vrg_ctx *ctx, int enable);
 /* Accumulated device time and launch count of kernel `name` since the last
- * reset; names: "trace_mask", "trace_closest", "direct_luxels",
- * "direct_points", "transfer_rows", "transfer_gather", "bounce_spmv",
- * "bounce_reduce", "batch_queue". */
+ * reset; names: "trace_mask", "trace_closest", "trace_lines",
+ * "direct_luxels", "direct_points", "transfer_rows", "transfer_gather",
+ * "bounce_init", "bounce_spmv", "bounce_reduce", "batch_gather",
+ * "batch_bounce_init", "batch_spmv", "batch_reduce", "relight_gather". */
 int vrg_ctx_kernel_stats(vrg_ctx *ctx, const char *name, double *total_ms, int64_t *launches);
 int vrg_ctx_reset_stats(vrg_ctx *ctx);
 /* Kernels launched by this context since creation (all names). */
 int64_t vrg_ctx_launch_count(const vrg_ctx *ctx);
 
 /* Per-scene-size autotuning (no reference counterpart).  Tuned launch
- * sites ("trace_mask", "trace_mask_hit", "direct_luxels") offer variants
- * that give identical results; the first launch in a bucket
- * "<site>/t<log2 triangles>/n<log2 work items>" times each once on the real
+ * sites ("trace_mask", "trace_mask_hit", "direct_luxels", "transfer_rows",
+ * "bounce_spmv") offer variants that give identical results (the bounce
+ * variants: the same sums); the first launch in a bucket
+ * "<site>/t<log2 triangles>/n<log2 work items>" times each twice on the real
  * input and keeps the fastest.  On by default; off, or inside a stream
  * capture, an untuned bucket runs variant 0. */
 int vrg_ctx_set_autotune(vrg_ctx *ctx, int enable);

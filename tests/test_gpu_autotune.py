@@ -69,8 +69,8 @@ def test_direct_variants_identical_and_choice_recorded(gpu_ctx, tmp_path):
     assert gpu_ctx.autotune_choice(key)[0] == -1
     rgb0, rays0 = env.gather_direct_light(supersamples=4, seed=2)  # tunes this bucket
     v, ms = gpu_ctx.autotune_choice(key)
-    assert v in (0, 1, 2, 3) and len(ms) == 4
-    for v in range(4):
+    assert v in range(5) and len(ms) == 5
+    for v in range(5):
         _force(gpu_ctx, tmp_path, key, v)
         rgb, rays = env.gather_direct_light(supersamples=4, seed=2)
         assert rays == rays0

@@ -26,7 +26,11 @@ constexpr int kThreads = 128;
 // Optional second segment: npts sample points (pts, nrm: 3 floats each)
 // after the luxel samples, written to pout -- the leaf-patch points of a
 // bake, which alone are too few to fill the GPU.
-template <int FETCH, bool STREAM = false>
+// TILE walks each face's luxels in 4 x 2 tiles instead of row order, so a
+// warp's 8 luxels cover 64 x 32 units of the face instead of a 128-unit
+// strip (the output is the same: each luxel is still written by the lane
+// holding its first sample).
+template <int FETCH, bool STREAM = false, bool TILE = false>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
@@ -48,25 +52,55 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
         const int64_t gi = (int64_t)wb + lane;
         float r = 0.0f, g = 0.0f, b = 0.0f;
         int64_t lux = 0;
-        if (gi >= nsamp && gi < total) {
+        // one sample point per lane: a luxel supersample or an extra point;
+        // a single gather_point call site keeps the kernel's code compact
+        float px = 0.0f, py = 0.0f, pz = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f;
+        const bool is_pt = gi >= nsamp && gi < total;
+        if (is_pt) {
             const int64_t i = gi - nsamp;
-            gather_point<kSkyTrace, STREAM>(s, lights, nl, __ldg(pts + 3 * i), __ldg(pts + 3 * i + 1),
-                                            __ldg(pts + 3 * i + 2), __ldg(nrm + 3 * i), __ldg(nrm + 3 * i + 1),
-                                            __ldg(nrm + 3 * i + 2), r, g, b, rays);
-            pout[3 * i] = r;
-            pout[3 * i + 1] = g;
-            pout[3 * i + 2] = b;
+            px = __ldg(pts + 3 * i);
+            py = __ldg(pts + 3 * i + 1);
+            pz = __ldg(pts + 3 * i + 2);
+            nx = __ldg(nrm + 3 * i);
+            ny = __ldg(nrm + 3 * i + 1);
+            nz = __ldg(nrm + 3 * i + 2);
         } else if (gi < nsamp) {
             lux = gi / ss;
             const int k = (int)(gi - lux * ss);
             const int f = find_face(off, nfaces, lux);
             const FaceRec fr = faces[f];
-            const int64_t local = lux - __ldg(off + f);
-            const int iv = (int)(local / fr.nu), iu = (int)(local - (int64_t)iv * fr.nu);
-            float px, py, pz;
+            int64_t local = lux - __ldg(off + f);
+            int iv, iu;
+            if (TILE) {
+                // ordinal `local` -> (row, column) in 4 x 2 tiles, left to right
+                // within bands of two rows (one row in the last band of an odd
+                // face); the last tile of a band may be narrower
+                const int nu = fr.nu;
+                const int band = (int)(local / (2 * (int64_t)nu));
+                const int h = (2 * band + 1 < fr.nv) ? 2 : 1;
+                const int r = (int)(local - (int64_t)band * 2 * nu);
+                const int c = r / (4 * h);
+                const int q = r - c * 4 * h;
+                const int w = min(4, nu - 4 * c);
+                iu = 4 * c + q % w;
+                iv = 2 * band + q / w;
+                local = (int64_t)iv * nu + iu;
+                lux = __ldg(off + f) + local;
+            } else {
+                iv = (int)(local / fr.nu);
+                iu = (int)(local - (int64_t)iv * fr.nu);
+            }
             luxel_sample(fr, lux, iu, iv, k, ss, seed, px, py, pz);
-            gather_point<kSkyTrace, STREAM>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g,
-                                            b, rays);
+            nx = fr.normal.x;
+            ny = fr.normal.y;
+            nz = fr.normal.z;
+        }
+        if (gi < total) gather_point<kSkyTrace, STREAM>(s, lights, nl, px, py, pz, nx, ny, nz, r, g, b, rays);
+        if (is_pt) {
+            const int64_t i = gi - nsamp;
+            pout[3 * i] = r;
+            pout[3 * i + 1] = g;
+            pout[3 * i + 2] = b;
         }
         if (ss == 4) {
             const float r1 = __shfl_down_sync(0xffffffffu, r, 1), r2 = __shfl_down_sync(0xffffffffu, r, 2), r3 = __shfl_down_sync(0xffffffffu, r, 3);
@@ -154,8 +188,8 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     const DevScene s = scene_view(env);
     const DevLight *lights = env->d_lights.as<DevLight>();
     const int nl = (int)env->lights.size();
-    // variants: samples claimed per warp (32, 64, 128), and 32 with the leaf
-    // records kept out of L1; picked per bucket
+    // variants: samples claimed per warp (32, 64, 128), 32 with the leaf
+    // records kept out of L1, 32 in 4 x 2 luxel tiles; picked per bucket
     auto launch = [&](int v) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
         if (e == cudaSuccess && d_rays) e = cudaMemsetAsync(d_rays, 0, 8, ctx->stream);
@@ -168,13 +202,15 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
             k_direct_luxels<64><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else if (v == 2)
             k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else
+        else if (v == 3)
             k_direct_luxels<32, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+        else
+            k_direct_luxels<32, false, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 4, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 5, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

@@ -4,10 +4,11 @@
 // same result with different trade-offs (how many triangle planes a walk
 // fetches at once, how much work a warp claims at a time).  The first launch
 // in a scene-size bucket (log2 of the triangle count and of the work size)
-// runs every variant once on the real input, timed with CUDA events, and
+// runs every variant twice on the real input, timed with CUDA events, and
 // keeps the fastest; later launches in that bucket use it directly.  Inside
 // a stream capture, or with tuning switched off, an untuned bucket runs
 // variant 0.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -50,15 +51,20 @@ int tune_pick(vrg_ctx *ctx, const std::string &key, int nvar,
     VRG_CUDA(ctx, cudaEventCreate(&b));
     std::vector<double> ms(nvar, 0.0);
     cudaError_t err = launch(0);  // warm-up: first touch of code and data
-    for (int i = 0; i < nvar && err == cudaSuccess; i++) {
-        err = cudaEventRecord(a, ctx->stream);
-        if (err == cudaSuccess) err = launch(i);
-        if (err == cudaSuccess) err = cudaEventRecord(b, ctx->stream);
-        if (err == cudaSuccess) err = cudaEventSynchronize(b);
-        float t = 0.0f;
-        if (err == cudaSuccess) err = cudaEventElapsedTime(&t, a, b);
-        ms[i] = t;
-    }
+    // two passes, the second in reverse order, keeping each variant's
+    // faster run: a one-off slow launch or a drift of the clock over the
+    // passes does not decide the choice
+    for (int pass = 0; pass < 2; pass++)
+        for (int j = 0; j < nvar && err == cudaSuccess; j++) {
+            const int i = pass == 0 ? j : nvar - 1 - j;
+            err = cudaEventRecord(a, ctx->stream);
+            if (err == cudaSuccess) err = launch(i);
+            if (err == cudaSuccess) err = cudaEventRecord(b, ctx->stream);
+            if (err == cudaSuccess) err = cudaEventSynchronize(b);
+            float t = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&t, a, b);
+            ms[i] = pass == 0 ? t : std::min<double>(ms[i], t);
+        }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (err != cudaSuccess) return cuda_fail(ctx, err, "autotune");
