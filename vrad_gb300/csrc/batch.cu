@@ -91,8 +91,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_batch_gather(
                 const int k = (int)(local - lux * ss);
                 const int f = find_face(d->luxel_off, d->nfaces, lux);
                 const FaceRec fr = d->faces[f];
-                const int64_t within = lux - __ldg(d->luxel_off + f);
-                const int iv = (int)(within / fr.nu), iu = (int)(within - (int64_t)iv * fr.nu);
+                int iu, iv;  // the face's luxels in 4 x 2 tiles
+                tile_luxel(lux - __ldg(d->luxel_off + f), fr.nu, fr.nv, iu, iv);
+                lux = __ldg(d->luxel_off + f) + (int64_t)iv * fr.nu + iu;
                 float px, py, pz;
                 luxel_sample(fr, lux, iu, iv, k, ss, seed, px, py, pz);
                 gather_point<kSkyTrace>(scene, d->lights, d->nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z,

@@ -26,10 +26,9 @@ constexpr int kThreads = 128;
 // Optional second segment: npts sample points (pts, nrm: 3 floats each)
 // after the luxel samples, written to pout -- the leaf-patch points of a
 // bake, which alone are too few to fill the GPU.
-// TILE walks each face's luxels in 4 x 2 tiles instead of row order, so a
-// warp's 8 luxels cover 64 x 32 units of the face instead of a 128-unit
-// strip (the output is the same: each luxel is still written by the lane
-// holding its first sample).
+// TILE walks each face's luxels in 4 x 2 tiles (tile_luxel) instead of row
+// order; the output is the same, each luxel written by the lane holding its
+// first sample.
 template <int FETCH, bool STREAM = false, bool TILE = false>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
@@ -72,19 +71,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             int64_t local = lux - __ldg(off + f);
             int iv, iu;
             if (TILE) {
-                // ordinal `local` -> (row, column) in 4 x 2 tiles, left to right
-                // within bands of two rows (one row in the last band of an odd
-                // face); the last tile of a band may be narrower
-                const int nu = fr.nu;
-                const int band = (int)(local / (2 * (int64_t)nu));
-                const int h = (2 * band + 1 < fr.nv) ? 2 : 1;
-                const int r = (int)(local - (int64_t)band * 2 * nu);
-                const int c = r / (4 * h);
-                const int q = r - c * 4 * h;
-                const int w = min(4, nu - 4 * c);
-                iu = 4 * c + q % w;
-                iv = 2 * band + q / w;
-                local = (int64_t)iv * nu + iu;
+                tile_luxel(local, fr.nu, fr.nv, iu, iv);
+                local = (int64_t)iv * fr.nu + iu;
                 lux = __ldg(off + f) + local;
             } else {
                 iv = (int)(local / fr.nu);

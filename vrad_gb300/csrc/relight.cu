@@ -111,11 +111,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_relight_gather(
                 local = gi - __ldg(list.samp_off + k);
                 lux = __ldg(luxel_off + f) + local / ss;
             }
-            const int64_t gsamp = lux * ss + (int)(local % ss);
             const int kk = (int)(local % ss);
             const FaceRec fr = faces[f];
-            const int64_t within = lux - __ldg(luxel_off + f);
-            const int iv = (int)(within / fr.nu), iu = (int)(within - (int64_t)iv * fr.nu);
+            int iu, iv;  // the face's luxels in 4 x 2 tiles
+            tile_luxel(lux - __ldg(luxel_off + f), fr.nu, fr.nv, iu, iv);
+            lux = __ldg(luxel_off + f) + (int64_t)iv * fr.nu + iu;
+            const int64_t gsamp = lux * ss + kk;
             float px, py, pz;
             luxel_sample(fr, lux, iu, iv, kk, ss, seed, px, py, pz);
             gather_point<SKY>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g,

@@ -184,6 +184,24 @@ __device__ __forceinline__ void luxel_sample(const FaceRec &f, int64_t lux, int 
     pz = radd(radd(radd(f.corner.z, rmul(f.u.z, su)), rmul(f.v.z, sv)), rmul(f.normal.z, kSampleOffset));
 }
 
+// Walk order of a face's luxels in 4 x 2 tiles: ordinal o (0 .. nu*nv-1)
+// -> (iu, iv), tiles left to right within bands of two rows (one row in the
+// last band of a face with odd nv), the last tile of a band narrower when
+// nu is not a multiple of 4.  A bijection, so every luxel is visited once;
+// a warp's 8 consecutive luxels then cover a 64 x 32-unit patch of the face
+// instead of a 128-unit strip, and its lanes' shadow lines stay together
+// longer.
+__device__ __forceinline__ void tile_luxel(int64_t o, int nu, int nv, int &iu, int &iv) {
+    const int band = (int)(o / (2 * (int64_t)nu));
+    const int h = (2 * band + 1 < nv) ? 2 : 1;
+    const int r = (int)(o - (int64_t)band * 2 * nu);
+    const int c = r / (4 * h);
+    const int q = r - c * 4 * h;
+    const int w = min(4, nu - 4 * c);
+    iu = 4 * c + q % w;
+    iv = 2 * band + q / w;
+}
+
 __device__ __forceinline__ int find_face(const int64_t *__restrict__ off, int nfaces, int64_t lux) {
     int lo = 0, hi = nfaces - 1;
     while (lo < hi) {
