@@ -165,6 +165,21 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The slowest rank's time: every rank ran the same replica workload."""
+    import torch
+    import torch.distributed as td
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, max_ms: float) -> float:
+    """Units processed by all replicas (M/s) over the slowest rank's time."""
+    return units_per_rank * world / (max_ms * 1e-3) / 1e6
+
+
 def _l2_read_gbs(device: int):
     """L2 read bandwidth: a 32 MiB buffer read 200 times in one launch
     (libvrgprobe.so, built beside the product library)."""
@@ -291,10 +306,8 @@ def run_gpu(args, rank, world, local_rank):
     kms, kn = lib_ctx.kernel_stats(kernel)
     lib_ctx.set_timing(False)
     if dist:
-        t = torch.tensor([total_ms], device=dev)
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = units * args.steps * world / (total_ms * 1e-3) / 1e6
+        total_ms = max_over_ranks(total_ms, dev)
+    value = whole_job_rate(units * args.steps, world, total_ms)
 
     # end to end through the host-buffer C ABI (pinned host memory)
     for _ in range(2):

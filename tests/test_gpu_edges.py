@@ -1,0 +1,81 @@
+"""Edge cases through the C ABI on the GPU: empty batches, ragged sizes
+around the 32-line mask words and warp claims, lines starting on a
+triangle's plane, and a relight that changes nothing."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal, small_lit_scene
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env_and_oracle(gpu_ctx, oracle, anyhit_scene):
+    from vrad_gb300.environment import Environment
+
+    env = Environment(gpu_ctx)
+    env.add_triangles(anyhit_scene.xyz, anyhit_scene.ids)
+    env.SetupAccelerationStructure()
+    return env, oracle.Scene(anyhit_scene.xyz, anyhit_scene.ids)
+
+
+def test_empty_batches(env_and_oracle):
+    env, _ = env_and_oracle
+    z = np.zeros((0, 3), np.float32)
+    assert env.occlusion_mask(z, z).shape == (0,)
+    m, h, t = env.occlusion_mask(z, z, closest=True)
+    assert m.shape == h.shape == t.shape == (0,)
+    h, t = env.trace_closest(z, z, 0.0, 1.0)
+    assert h.shape == (0,)
+    assert env.test_line_does_hit_sky(z, z).shape == (0,)
+
+
+@pytest.mark.parametrize("n", [1, 31, 32, 33, 127, 4097, 100003])
+def test_ragged_line_counts(env_and_oracle, anyhit_scene, n):
+    env, osc = env_and_oracle
+    a, b = anyhit_scene.starts[:n], anyhit_scene.stops[:n]
+    mask, hit, t = env.occlusion_mask(a, b, closest=True)
+    rmask, rhit, rt = osc.occlusion_mask(a, b, threads=16, closest=True)
+    assert np.array_equal(mask, rmask)
+    assert np.array_equal(hit, rhit) and bits_equal(t, rt)
+
+
+def test_lines_from_triangle_planes(env_and_oracle, anyhit_scene):
+    # lines that start exactly on a box face (t = 0 hits) and lines that
+    # end exactly on one (t = len, excluded by tmin <= t < tmax)
+    env, osc = env_and_oracle
+    xyz = anyhit_scene.xyz.reshape(-1, 3, 3)
+    rng = np.random.default_rng(5)
+    pick = rng.choice(len(xyz), size=4000, replace=False)
+    on = xyz[pick].mean(axis=1).astype(np.float32)  # centroids lie on their triangles
+    far = rng.uniform(1, 4095, (4000, 3)).astype(np.float32)
+    for a, b in ((on, far), (far, on)):
+        mask = env.occlusion_mask(a, b)
+        assert np.array_equal(mask, osc.occlusion_mask(a, b, threads=16))
+
+
+def test_relight_without_change_keeps_the_bake(gpu_ctx):
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment, make_light
+
+    lit = small_lit_scene(48, seed=21)
+    env = Environment(gpu_ctx)
+    env.add_triangles(lit.xyz, lit.ids)
+    env.SetupAccelerationStructure()
+    env.set_faces(lit)
+    env.set_lights(lit.lights)
+    P = env.make_patches()
+    env.make_transfers(scenes.transfer_directions(128))
+    env.relight_prepare(4, 3, 100, 1e-4)
+    before = env.get_bake(P["n_leaves"])
+    li = lit.lights[0]
+    same = make_light(li.type, li.origin, li.intensity, li.normal, **li.keys)
+    env.relight([], max_iters=50, rel_tol=1e-4)
+    env.relight([(0, same)], max_iters=50, rel_tol=1e-4)  # an edit to the same values
+    after = env.get_bake(P["n_leaves"])
+    assert np.array_equal(before["luxels"], after["luxels"])
+    assert np.array_equal(before["patch_direct"], after["patch_direct"])
+    scale = max(np.abs(before["patch_total"]).max(), 1e-30)
+    err = np.abs(after["patch_total"] - before["patch_total"]) / np.maximum(
+        np.abs(before["patch_total"]), 1e-6 * scale)
+    assert err.max() <= 1e-3
