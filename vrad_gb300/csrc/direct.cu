@@ -29,13 +29,14 @@ constexpr int kThreads = 128;
 // TILE walks each face's luxels in 4 x 2 tiles (tile_luxel) instead of row
 // order; the output is the same, each luxel written by the lane holding its
 // first sample.
-template <int FETCH, bool STREAM = false, bool TILE = false>
+template <int FETCH, int OPT = 0, bool TILE = false>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
     float *__restrict__ out, const float *__restrict__ pts, const float *__restrict__ nrm, int64_t npts,
     float *__restrict__ pout, unsigned long long *__restrict__ ray_count,
     unsigned long long *__restrict__ work) {
+    if (OPT & kOptTop) stage_top(s);
     const int64_t nsamp = nlux * ss;
     const int64_t total = nsamp + npts;
     const int lane = threadIdx.x & 31;
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             ny = fr.normal.y;
             nz = fr.normal.z;
         }
-        if (gi < total) gather_point<kSkyTrace, STREAM>(s, lights, nl, px, py, pz, nx, ny, nz, r, g, b, rays);
+        if (gi < total) gather_point<kSkyTrace, OPT>(s, lights, nl, px, py, pz, nx, ny, nz, r, g, b, rays);
         if (is_pt) {
             const int64_t i = gi - nsamp;
             pout[3 * i] = r;
@@ -177,7 +178,8 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     const DevLight *lights = env->d_lights.as<DevLight>();
     const int nl = (int)env->lights.size();
     // variants: samples claimed per warp (32, 64, 128), 32 with the leaf
-    // records kept out of L1, 32 in 4 x 2 luxel tiles; picked per bucket
+    // records kept out of L1, 32 in 4 x 2 luxel tiles without and with the
+    // top of the tree in shared memory; picked per bucket
     auto launch = [&](int v) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
         if (e == cudaSuccess && d_rays) e = cudaMemsetAsync(d_rays, 0, 8, ctx->stream);
@@ -191,14 +193,16 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
         else if (v == 2)
             k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else if (v == 3)
-            k_direct_luxels<32, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+            k_direct_luxels<32, kOptStream><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+        else if (v == 4)
+            k_direct_luxels<32, 0, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else
-            k_direct_luxels<32, false, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+            k_direct_luxels<32, kOptTop, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 5, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 6, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

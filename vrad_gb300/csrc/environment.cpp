@@ -115,6 +115,34 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         memcpy(&sbits, &env->tree.split[i], 4);
         nodes[i] = make_uint2(env->tree.children[i], sbits);
     }
+    // top table: breadth-first from the root, a pair of children at a
+    // time, while it fits; children words of nodes whose children made it
+    // into the table point into the table (index | kTopRef)
+    std::vector<uint2> top;
+    if (nn < (size_t)kTopRef) {
+        std::vector<int64_t> at(nn, -1);
+        std::vector<uint32_t> order;  // node array index of each table entry
+        top.push_back(nodes[0]);
+        order.push_back(0);
+        at[0] = 0;
+        for (size_t q = 0; q < order.size(); q++) {
+            const uint32_t x = order[q];
+            if ((nodes[x].x & 3u) == kLeaf || top.size() + 2 > (size_t)kTopNodes) continue;
+            const uint32_t left = nodes[x].x >> 2;
+            for (uint32_t c = 0; c < 2; c++) {
+                at[left + c] = (int64_t)top.size();
+                top.push_back(nodes[left + c]);
+                order.push_back(left + c);
+            }
+        }
+        for (size_t t = 0; t < top.size(); t++) {
+            const uint32_t x = order[t];
+            if ((nodes[x].x & 3u) == kLeaf) continue;
+            const int64_t l = at[nodes[x].x >> 2];
+            if (l >= 0) top[t].x = (nodes[x].x & 3u) | (((uint32_t)l | kTopRef) << 2);
+        }
+    }
+    env->ntop = (uint32_t)top.size();
     const size_t nr1 = nr ? nr : 1;
     std::vector<float4> leaf(3 * nr1, make_float4(0, 0, 0, 0));
     for (size_t r = 0; r < nr; r++) {
@@ -132,6 +160,10 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     VRG_CUDA(ctx, env->d_nodes.reserve(nn * sizeof(uint2)));
     VRG_CUDA(ctx, env->d_leaf_tris.reserve(leaf.size() * sizeof(float4)));
     VRG_CUDA(ctx, env->d_tri_ids.reserve((n ? n : 1) * sizeof(int32_t)));
+    VRG_CUDA(ctx, env->d_top.reserve(std::max<size_t>(top.size(), 1) * sizeof(uint2)));
+    if (!top.empty())
+        VRG_CUDA(ctx, cudaMemcpyAsync(env->d_top.ptr, top.data(), top.size() * sizeof(uint2),
+                                      cudaMemcpyHostToDevice, ctx->stream));
     VRG_CUDA(ctx, cudaMemcpyAsync(env->d_nodes.ptr, nodes.data(), nn * sizeof(uint2),
                                   cudaMemcpyHostToDevice, ctx->stream));
     VRG_CUDA(ctx, cudaMemcpyAsync(env->d_leaf_tris.ptr, leaf.data(), leaf.size() * sizeof(float4),

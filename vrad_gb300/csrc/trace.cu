@@ -23,13 +23,14 @@ __device__ __forceinline__ void load3(const float *p, int64_t i, float &x, float
 // a device counter zeroed before the launch).  The occlusion bit goes into
 // the 1-bit mask with an atomic OR (the mask is zeroed before the launch).
 // WANT_HIT also writes the closest hit of the normalised segment.
-template <bool WANT_HIT, int LB, bool STREAM = false>
+template <bool WANT_HIT, int LB, int OPT = 0>
 __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
                                                           int32_t skip, uint32_t *__restrict__ mask,
                                                           int32_t *__restrict__ hit,
                                                           float *__restrict__ thit,
                                                           unsigned long long *__restrict__ work) {
+    if (OPT & kOptTop) stage_top(s);
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -55,7 +56,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
                     load3(start, i, sx, sy, sz);
                     load3(stop, i, ex, ey, ez);
                     p = plan_line(s, make_line(sx, sy, sz, ex, ey, ez));
-                    active = !p.trivial && trace_init(s, p.ray, p.rp, p.slack, 0.0f, p.len, st);
+                    active = !p.trivial && trace_init(s, p.ray, p.rp, p.slack, 0.0f, p.len, st, root_ref<OPT>(s));
                     if (!active && WANT_HIT) {
                         hit[ri] = -1;
                         thit[ri] = kInf;
@@ -65,8 +66,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
         }
         if (active) {
             const bool done =
-                WANT_HIT ? trace_step<kClosest, LB, STREAM>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
-                         : trace_step<kSkyOcc, LB, STREAM>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
+                WANT_HIT ? trace_step<kClosest, LB, OPT>(s, p.ray, p.rp, 0.0f, p.len, skip, 0.0f, st)
+                         : trace_step<kSkyOcc, LB, OPT>(s, p.ray, p.rp, 0.0f, p.len, skip, p.any_limit, st);
             if (done) {
                 active = false;
                 bool occ;
@@ -97,13 +98,14 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
 // MINB is the resident-block hint of __launch_bounds__ (register cap).
 // Leaf order, pruning and tie rule are those of trace_step: same verdicts
 // and closest hits.
-template <bool WANT_HIT, int THRESH, bool VOTE, int MINB, bool STREAM = false>
+template <bool WANT_HIT, int THRESH, bool VOTE, int MINB, int OPT = 0>
 __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const float *__restrict__ start,
                                                           const float *__restrict__ stop, int64_t n,
                                                           int32_t skip, uint32_t *__restrict__ mask,
                                                           int32_t *__restrict__ hit,
                                                           float *__restrict__ thit,
                                                           unsigned long long *__restrict__ work) {
+    if (OPT & kOptTop) stage_top(s);
     constexpr int MODE = WANT_HIT ? kClosest : kSkyOcc;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -156,8 +158,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
                         go = t0 <= t1;
                     }
                     if (go) {
-                        node = 0;
-                        nd = __ldg(&s.nodes[0]);
+                        node = root_ref<OPT>(s);
+                        nd = fetch_node<OPT>(s, node);
                         active = true;
                     } else if (WANT_HIT) {
                         hit[ri] = -1;
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
             lend = lpos + (uint32_t)__uint_as_float(nd.y);
             if (lpos == lend) {  // empty leaf
                 if (pop_next<MODE>(stk, sp, best_t, node, t0, t1))
-                    nd = __ldg(&s.nodes[node]);
+                    nd = fetch_node<OPT>(s, node);
                 else
                     done = true;
             }
@@ -187,18 +189,18 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
             run_node = run_node && cn > ct;
         }
         if (run_tri) {
-            const float4 w0 = leaf_load<STREAM>(s.leaf_planes + lpos);
-            if (tri_test<MODE, STREAM>(s, ray, 0.0f, len, skip, any_limit, w0, lpos, best, best_t)) {
+            const float4 w0 = leaf_load<OPT>(s.leaf_planes + lpos);
+            if (tri_test<MODE, OPT>(s, ray, 0.0f, len, skip, any_limit, w0, lpos, best, best_t)) {
                 done = true;
             } else if (++lpos == lend) {
                 if (pop_next<MODE>(stk, sp, best_t, node, t0, t1))
-                    nd = __ldg(&s.nodes[node]);
+                    nd = fetch_node<OPT>(s, node);
                 else
                     done = true;
             }
         } else if (run_node) {
             node = inner_step(rp, nd, t0, t1, stk, sp);
-            nd = __ldg(&s.nodes[node]);
+            nd = fetch_node<OPT>(s, node);
         }
         if (done) {
             active = false;
@@ -307,22 +309,25 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // Variants of the shadow-line walk, picked per scene-size bucket: per-lane
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
 // lanes, with or without the vote, at the default or a 40-register cap,
-// leaf records kept out of L1 or not).
+// leaf records kept out of L1 or not, top of the tree in shared memory or
+// not).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
     k_trace_unit<false, 4, false, 12>, k_trace_unit<false, 4, true, 12>,
-    k_trace_unit<false, 4, false, 1, true>, k_trace_unit<false, 8, false, 1, true>,
-    k_trace_mask<false, 1, true>,
+    k_trace_unit<false, 4, false, 1, kOptStream>, k_trace_unit<false, 8, false, 1, kOptStream>,
+    k_trace_mask<false, 1, kOptStream>,
+    k_trace_unit<false, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<false, 8, false, 1, kOptStream | kOptTop>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
     k_trace_unit<true, 4, true, 1>, k_trace_unit<true, 8, true, 1>,
     k_trace_unit<true, 4, false, 12>, k_trace_unit<true, 4, true, 12>,
-    k_trace_unit<true, 4, false, 1, true>, k_trace_unit<true, 8, false, 1, true>,
-    k_trace_mask<true, 1, true>,
+    k_trace_unit<true, 4, false, 1, kOptStream>, k_trace_unit<true, 8, false, 1, kOptStream>,
+    k_trace_mask<true, 1, kOptStream>,
+    k_trace_unit<true, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<true, 8, false, 1, kOptStream | kOptTop>,
 };
-constexpr int kMaskVariants = 9;
+constexpr int kMaskVariants = 11;
 
 }  // namespace
 
@@ -332,6 +337,8 @@ DevScene scene_view(const vrg_env *env) {
     s.leaf_planes = env->d_leaf_tris.as<float4>();
     s.leaf_edges = s.leaf_planes + std::max<size_t>(env->tree.refs.size(), 1);
     s.tri_ids = env->d_tri_ids.as<int32_t>();
+    s.top = env->d_top.as<uint2>();
+    s.ntop = env->ntop;
     s.g = env->geom;
     return s;
 }

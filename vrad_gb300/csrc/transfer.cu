@@ -19,9 +19,9 @@ namespace {
 
 // One block per row: trace the k rays, sort the k target ids in shared
 // memory (bitonic), then a block scan compacts runs into (col, count).  NT
-// threads per block (at most k); STREAM loads the leaf records without
+// threads per block (at most k); OPT & kOptStream loads the leaf records without
 // allocating in L1.
-template <int NT, bool STREAM>
+template <int NT, int OPT>
 __global__ void __launch_bounds__(NT) k_transfer_rows(
     DevScene s, const LeafInfo *__restrict__ leaves, const FaceRec *__restrict__ faces,
     const PatchNode *__restrict__ pnodes, const int32_t *__restrict__ face_root,
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(NT) k_transfer_rows(
             const float dz = radd(radd(rmul(lx, t1z), rmul(ly, t2z)), rmul(lz, nz));
             float t;
             const int32_t h =
-                trace_ray<kClosest, STREAM>(s, Ray{qx, qy, qz, dx, dy, dz}, 0.0f, kMaxTraceLength, -1, &t);
+                trace_ray<kClosest, OPT>(s, Ray{qx, qy, qz, dx, dy, dz}, 0.0f, kMaxTraceLength, -1, &t);
             int32_t target = -1;
             if (h >= 0) {
                 const int32_t g = __ldg(tri_face + h);
@@ -216,8 +216,8 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k) {
     using RowKernel = void (*)(DevScene, const LeafInfo *, const FaceRec *, const PatchNode *, const int32_t *,
                                const int32_t *, const float *, int, int64_t, int64_t, int32_t *, int32_t *,
                                int32_t *);
-    const RowKernel kvar[4] = {k_transfer_rows<256, false>, k_transfer_rows<512, false>,
-                               k_transfer_rows<256, true>, k_transfer_rows<512, true>};
+    const RowKernel kvar[4] = {k_transfer_rows<256, 0>, k_transfer_rows<512, 0>,
+                               k_transfer_rows<256, kOptStream>, k_transfer_rows<512, kOptStream>};
     const int vthreads[4] = {256, 512, 256, 512};
     for (int v = 0; v < 4; v++)
         VRG_CUDA(ctx, cudaFuncSetAttribute(kvar[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -45,8 +45,17 @@ struct DevScene {
     const float4 *leaf_planes;  // 1 float4 per TriangleIndexList entry
     const float4 *leaf_edges;   // 2 float4 per TriangleIndexList entry
     const int32_t *tri_ids;     // NTriangleID per triangle index
+    const uint2 *top;           // top levels of the tree in breadth-first order (see kTopRef)
+    uint32_t ntop;              // entries of `top` (0: none)
     SceneGeom g;
 };
+
+// The top table holds the first kTopNodes nodes of a breadth-first walk from
+// the root, children pairs kept adjacent.  A child word there whose index
+// has kTopRef set points into the table instead of the node array, so a
+// walk that stages the table in shared memory reads the top levels there.
+constexpr int kTopNodes = 512;
+constexpr uint32_t kTopRef = 1u << 28;
 
 // Lightmapped face, 80 bytes.
 struct alignas(16) FaceRec {

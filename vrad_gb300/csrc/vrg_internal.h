@@ -119,6 +119,8 @@ struct vrg_env {
 
     // device scene
     vrg::DevBuf d_nodes, d_leaf_tris, d_tri_ids, d_tri_normals;
+    vrg::DevBuf d_top;       // top levels of the tree (kTopNodes entries at most)
+    uint32_t ntop = 0;
 
     // lights
     std::vector<vrg_light> lights;

@@ -26,6 +26,35 @@ __device__ __forceinline__ float pick3(int a, float x, float y, float z) {
 }
 
 constexpr int32_t kTraceIdSky = 0x01000000;
+
+// Walk options (template bits): kOptStream loads leaf records without
+// allocating in L1; kOptTop reads the top levels of the tree from a copy in
+// shared memory (stage_top).
+constexpr int kOptStream = 1;
+constexpr int kOptTop = 2;
+
+// Shared-memory copy of the scene's top table, for kernels walking with
+// kOptTop (allocated only in kernels that use it).
+static __shared__ uint2 g_top_nodes[kTopNodes];
+
+// Every thread of the block calls this once, before its first walk.
+__device__ __forceinline__ void stage_top(const DevScene &s) {
+    for (uint32_t i = threadIdx.x; i < s.ntop; i += blockDim.x) g_top_nodes[i] = __ldg(&s.top[i]);
+    __syncthreads();
+}
+
+// The node a walk starts from, and a node record by reference: with kOptTop
+// a reference carrying kTopRef is read from the shared copy.
+template <int OPT>
+__device__ __forceinline__ uint32_t root_ref(const DevScene &s) {
+    return ((OPT & kOptTop) && s.ntop > 0) ? kTopRef : 0u;
+}
+
+template <int OPT>
+__device__ __forceinline__ uint2 fetch_node(const DevScene &s, uint32_t ref) {
+    if ((OPT & kOptTop) && (ref & kTopRef)) return g_top_nodes[ref & (kTopRef - 1u)];
+    return __ldg(&s.nodes[ref]);
+}
 constexpr float kInf = __builtin_huge_valf();
 
 // Conservative slab half-thickness for split planes: a computed hit lies
@@ -117,11 +146,12 @@ struct TraceState {
 // Starts a walk; returns false when the ray misses the scene's padded box
 // (st.best = -1 then).
 __device__ __forceinline__ bool trace_init(const DevScene &s, const Ray &ray, const RayPre &rp,
-                                           float slack, float tmin, float tmax, TraceState &st) {
+                                           float slack, float tmin, float tmax, TraceState &st,
+                                           uint32_t root = 0u) {
     st.best = -1;
     st.best_t = kInf;
     st.sp = 0;
-    st.node = 0;
+    st.node = root;
     if (s.g.ntris == 0 || !(tmin <= tmax)) return false;
     st.t0 = tmin;
     st.t1 = tmax;
@@ -168,12 +198,12 @@ __device__ __forceinline__ uint32_t inner_step(const RayPre &rp, uint2 nd, float
 // when the walk ends here: any accepted hit in kAny mode, a hit before
 // any_limit in kSkyOcc mode.  The edge part is fetched only when the plane
 // hit is in range.
-// Leaf-record load; STREAM asks L1 not to keep the line (the leaf records
+// Leaf-record load; kOptStream asks L1 not to keep the line (the leaf records
 // of a large scene stream past L1, where they would evict the nodes and the
 // traversal stacks that are reused).
-template <bool STREAM>
+template <int OPT>
 __device__ __forceinline__ float4 leaf_load(const float4 *p) {
-    if (!STREAM) return __ldg(p);
+    if (!(OPT & kOptStream)) return __ldg(p);
     float4 v;
     asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
@@ -181,7 +211,7 @@ __device__ __forceinline__ float4 leaf_load(const float4 *p) {
     return v;
 }
 
-template <int MODE, bool STREAM = false>
+template <int MODE, int OPT = 0>
 __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
                                          int32_t skip, float any_limit, const float4 w0, size_t k,
                                          int32_t &best, float &best_t) {
@@ -191,9 +221,9 @@ __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, floa
     if (!(t >= tmin && t < tmax)) return false;
     if (MODE != kAny && !(t <= best_t)) return false;
     const float4 *ed = s.leaf_edges + 2 * k;
-    const float4 w2 = leaf_load<STREAM>(ed + 1);
+    const float4 w2 = leaf_load<OPT>(ed + 1);
     if (__float_as_int(w2.z) == skip) return false;
-    const float4 w1 = leaf_load<STREAM>(ed);
+    const float4 w1 = leaf_load<OPT>(ed);
     const uint32_t idx_drop = __float_as_uint(w2.w);
     const int drop = (int)(idx_drop & 3u);
     // kept axes (drop+1)%3, (drop+2)%3
@@ -224,7 +254,7 @@ __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, floa
 // Tests the cnt triangles of a leaf (TriangleIndexList[start .. start+cnt))
 // with tri_test; true when the walk ends here.  LB triangle planes are
 // fetched at a time so their loads overlap.
-template <int MODE, int LB, bool STREAM = false>
+template <int MODE, int LB, int OPT = 0>
 __device__ __forceinline__ bool leaf_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
                                           int32_t skip, float any_limit, uint32_t start, int cnt,
                                           int32_t &best, float &best_t) {
@@ -233,11 +263,11 @@ __device__ __forceinline__ bool leaf_test(const DevScene &s, const Ray &ray, flo
         float4 P[LB];
 #pragma unroll
         for (int j = 0; j < LB; j++)
-            if (k0 + j < cnt) P[j] = leaf_load<STREAM>(pl + k0 + j);
+            if (k0 + j < cnt) P[j] = leaf_load<OPT>(pl + k0 + j);
 #pragma unroll
         for (int j = 0; j < LB; j++) {
             if (k0 + j >= cnt) break;
-            if (tri_test<MODE, STREAM>(s, ray, tmin, tmax, skip, any_limit, P[j], (size_t)start + k0 + j,
+            if (tri_test<MODE, OPT>(s, ray, tmin, tmax, skip, any_limit, P[j], (size_t)start + k0 + j,
                                        best, best_t))
                 return true;
         }
@@ -265,19 +295,19 @@ __device__ __forceinline__ bool pop_next(const uint4 *stk, int &sp, float best_t
 // One step of the walk: descend to a leaf, test its triangles, pop the next
 // subtree that can still hold the answer.  Returns true when the walk is
 // over; the answer is st.best / st.best_t.
-template <int MODE, int LB = 1, bool STREAM = false>
+template <int MODE, int LB = 1, int OPT = 0>
 __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, const RayPre &rp,
                                            float tmin, float tmax, int32_t skip, float any_limit,
                                            TraceState &st) {
     uint32_t node = st.node;
     float t0 = st.t0, t1 = st.t1;
     int sp = st.sp;
-    uint2 nd = __ldg(&s.nodes[node]);
+    uint2 nd = fetch_node<OPT>(s, node);
     while ((nd.x & 3u) != 3u) {
         node = inner_step(rp, nd, t0, t1, st.stk, sp);
-        nd = __ldg(&s.nodes[node]);
+        nd = fetch_node<OPT>(s, node);
     }
-    if (leaf_test<MODE, LB, STREAM>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
+    if (leaf_test<MODE, LB, OPT>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
                             (int)__uint_as_float(nd.y), st.best, st.best_t))
         return true;
     if (!pop_next<MODE>(st.stk, sp, st.best_t, st.node, st.t0, st.t1))
@@ -287,24 +317,24 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
 }
 
 // A whole walk; returns the hit triangle index (-1 for none) and its t.
-template <int MODE, bool STREAM = false>
+template <int MODE, int OPT = 0>
 __device__ int32_t kd_trace(const DevScene &s, const Ray &ray, const RayPre &rp, float slack,
                             float tmin, float tmax, int32_t skip, float any_limit, float *t_out) {
     TraceState st;
-    if (trace_init(s, ray, rp, slack, tmin, tmax, st))
-        while (!trace_step<MODE, 1, STREAM>(s, ray, rp, tmin, tmax, skip, any_limit, st)) {
+    if (trace_init(s, ray, rp, slack, tmin, tmax, st, root_ref<OPT>(s)))
+        while (!trace_step<MODE, 1, OPT>(s, ray, rp, tmin, tmax, skip, any_limit, st)) {
         }
     *t_out = st.best_t;
     return st.best;
 }
 
 // Closest or first hit of one ray with its own setup.
-template <int MODE, bool STREAM = false>
+template <int MODE, int OPT = 0>
 __device__ __forceinline__ int32_t trace_ray(const DevScene &s, const Ray &ray, float tmin,
                                              float tmax, int32_t skip, float *t_out) {
     const float slack = ray_slack(s.g, ray.ox, ray.oy, ray.oz);
     const RayPre rp = ray_pre(ray, slack);
-    return kd_trace<MODE, STREAM>(s, ray, rp, slack, tmin, tmax, skip, 0.0f, t_out);
+    return kd_trace<MODE, OPT>(s, ray, rp, slack, tmin, tmax, skip, 0.0f, t_out);
 }
 
 // Shadow-line setup of TestLineDoesHitSky (raytracer/trace/testline.go:22-27):
@@ -365,13 +395,13 @@ __device__ __forceinline__ bool line_verdict(const DevScene &s, const LinePlan &
     return (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
 }
 
-template <bool STREAM = false>
+template <int OPT = 0>
 __device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
     const LinePlan p = plan_line(s, L);
     if (p.trivial) return false;
     float th;
     const int32_t h =
-        kd_trace<kSkyOcc, STREAM>(s, p.ray, p.rp, p.slack, 0.0f, p.len, skip, p.any_limit, &th);
+        kd_trace<kSkyOcc, OPT>(s, p.ray, p.rp, p.slack, 0.0f, p.len, skip, p.any_limit, &th);
     return line_verdict(s, p, h, th);
 }
 
