@@ -16,6 +16,22 @@ __device__ __forceinline__ void load3(const float *p, int64_t i, float &x, float
     z = __ldg(p + 3 * i + 2);
 }
 
+// The refill loops read each line's end points when a lane takes the line,
+// one lane at a time and out of step with its neighbours, so a line that is
+// not yet in L2 costs the lane a full HBM round trip.  At launch every
+// thread asks L2 for its share of the two end-point arrays (128-byte lines,
+// addresses inside the arrays only), so they stream in at full bandwidth
+// instead.
+__device__ __forceinline__ void prefetch_lines(const float *start, const float *stop, int64_t n) {
+    const int64_t bytes = 12 * n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x * 128;
+    const char *a = reinterpret_cast<const char *>(start), *b = reinterpret_cast<const char *>(stop);
+    for (int64_t off = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 128; off < bytes; off += stride) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a + off));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(b + off));
+    }
+}
+
 // Shadow lines with per-lane refill.  Independent lines diverge: some stop
 // at their first leaf, some cross the whole scene.  Each lane therefore
 // walks its own line one leaf at a time, and as soon as a lane's line is
@@ -31,6 +47,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_mask(DevScene s, const float
                                                           float *__restrict__ thit,
                                                           unsigned long long *__restrict__ work) {
     if (OPT & kOptTop) stage_top(s);
+    prefetch_lines(start, stop, n);
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -106,6 +123,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
                                                           float *__restrict__ thit,
                                                           unsigned long long *__restrict__ work) {
     if (OPT & kOptTop) stage_top(s);
+    prefetch_lines(start, stop, n);
     constexpr int MODE = WANT_HIT ? kClosest : kSkyOcc;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
