@@ -106,8 +106,9 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     g.scale = scale;
 
     // device upload: nodes (8 B), then in TriangleIndexList order the
-    // triangle planes (16 B each) followed by the edge parts (32 B each),
-    // NTriangleID per triangle
+    // triangle planes (16 B each) followed by the edge parts (32 B each:
+    // (e0, e3, e1, e4), (e2, e5, id, index << 2 | drop)), NTriangleID per
+    // triangle
     const size_t nn = env->tree.children.size(), nr = env->tree.refs.size();
     std::vector<uint2> nodes(nn);
     for (size_t i = 0; i < nn; i++) {
@@ -151,8 +152,9 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         memcpy(&id_bits, &t.id, 4);
         memcpy(&idx_bits, &t.idx_drop, 4);
         leaf[r] = make_float4(t.nx, t.ny, t.nz, t.d);
-        leaf[nr1 + 2 * r] = make_float4(t.e0, t.e1, t.e2, t.e3);
-        leaf[nr1 + 2 * r + 1] = make_float4(t.e4, t.e5, id_bits, idx_bits);
+        // edge part as pairs (e0, e3) (e1, e4) (e2, e5): b0 and b1 side by side
+        leaf[nr1 + 2 * r] = make_float4(t.e0, t.e3, t.e1, t.e4);
+        leaf[nr1 + 2 * r + 1] = make_float4(t.e2, t.e5, id_bits, idx_bits);
     }
     env->built = true;
     if (ctx->host_only) return VRG_OK;

@@ -328,7 +328,7 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
 // lanes, with or without the vote, at the default or a 40-register cap,
 // leaf records kept out of L1 or not, top of the tree in shared memory or
-// not).
+// not, packed triangle test).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
@@ -336,6 +336,7 @@ const MaskKernel kMaskOcc[] = {
     k_trace_unit<false, 4, false, 1, kOptStream>, k_trace_unit<false, 8, false, 1, kOptStream>,
     k_trace_mask<false, 1, kOptStream>,
     k_trace_unit<false, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<false, 8, false, 1, kOptStream | kOptTop>,
+    k_trace_unit<false, 4, false, 1, kOptStream | kOptPacked>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -344,8 +345,9 @@ const MaskKernel kMaskHit[] = {
     k_trace_unit<true, 4, false, 1, kOptStream>, k_trace_unit<true, 8, false, 1, kOptStream>,
     k_trace_mask<true, 1, kOptStream>,
     k_trace_unit<true, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<true, 8, false, 1, kOptStream | kOptTop>,
+    k_trace_unit<true, 4, false, 1, kOptStream | kOptPacked>,
 };
-constexpr int kMaskVariants = 11;
+constexpr int kMaskVariants = 12;
 
 }  // namespace
 
