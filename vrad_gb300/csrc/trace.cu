@@ -138,6 +138,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
     float t0 = 0.0f, t1 = 0.0f;
     int sp = 0;
     uint32_t lpos = 0, lend = 0;  // triangles of the current leaf still to test
+    float4 next_plane = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // kOptPipe: plane of lpos, loaded ahead
+    bool have_next = false;
     int32_t best = -1;
     float best_t = kInf;
     uint4 stk[kStackMax];
@@ -190,6 +192,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
         if (active && lpos == lend && (nd.x & 3u) == 3u) {
             lpos = nd.x >> 2;
             lend = lpos + (uint32_t)__uint_as_float(nd.y);
+            have_next = false;
             if (lpos == lend) {  // empty leaf
                 if (pop_next<MODE>(stk, sp, best_t, node, t0, t1))
                     nd = fetch_node<OPT>(s, node);
@@ -207,7 +210,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
             run_node = run_node && cn > ct;
         }
         if (run_tri) {
-            const float4 w0 = leaf_load<OPT>(s.leaf_planes + lpos);
+            float4 w0;
+            if (OPT & kOptPipe) {
+                w0 = have_next ? next_plane : leaf_load<OPT>(s.leaf_planes + lpos);
+                have_next = lpos + 1 < lend;
+                if (have_next) next_plane = leaf_load<OPT>(s.leaf_planes + lpos + 1);
+            } else {
+                w0 = leaf_load<OPT>(s.leaf_planes + lpos);
+            }
             if (tri_test<MODE, OPT>(s, ray, 0.0f, len, skip, any_limit, w0, lpos, best, best_t)) {
                 done = true;
             } else if (++lpos == lend) {
@@ -328,7 +338,7 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
 // lanes, with or without the vote, at the default or a 40-register cap,
 // leaf records kept out of L1 or not, top of the tree in shared memory or
-// not, packed triangle test).
+// not, packed triangle test, next plane loaded ahead).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
@@ -337,6 +347,7 @@ const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1, kOptStream>,
     k_trace_unit<false, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<false, 8, false, 1, kOptStream | kOptTop>,
     k_trace_unit<false, 4, false, 1, kOptStream | kOptPacked>,
+    k_trace_unit<false, 4, false, 1, kOptStream | kOptPacked | kOptPipe>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -346,8 +357,9 @@ const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1, kOptStream>,
     k_trace_unit<true, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<true, 8, false, 1, kOptStream | kOptTop>,
     k_trace_unit<true, 4, false, 1, kOptStream | kOptPacked>,
+    k_trace_unit<true, 4, false, 1, kOptStream | kOptPacked | kOptPipe>,
 };
-constexpr int kMaskVariants = 12;
+constexpr int kMaskVariants = 13;
 
 }  // namespace
 

@@ -33,6 +33,7 @@ constexpr int32_t kTraceIdSky = 0x01000000;
 constexpr int kOptStream = 1;
 constexpr int kOptTop = 2;
 constexpr int kOptPacked = 4;  // triangle test on packed float32x2 instructions
+constexpr int kOptPipe = 8;    // unit rounds: the next triangle's plane loads during this test
 
 // Shared-memory copy of the scene's top table, for kernels walking with
 // kOptTop (allocated only in kernels that use it).
