@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_closest(DevScene s, const fl
                 }
             }
         }
-        if (active && trace_step<kClosest, 1>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
+        if (active && trace_step<kClosest, 1, kOptPacked>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
             active = false;
             hit[ri] = st.best;
             thit[ri] = st.best_t;
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kThreads) k_test_lines(DevScene s, const float
         float sx, sy, sz, ex, ey, ez;
         load3(start, i, sx, sy, sz);
         load3(stop, i, ex, ey, ez);
-        frac[i] = line_occluded(s, make_line(sx, sy, sz, ex, ey, ez), skip) ? 0.0f : 1.0f;
+        frac[i] = line_occluded<kOptPacked>(s, make_line(sx, sy, sz, ex, ey, ez), skip) ? 0.0f : 1.0f;
     }
 }
 
