@@ -354,7 +354,7 @@ def run_gpu(args, rank, world, local_rank):
     tv, tms = lib_ctx.autotune_choice(tkey)
     # DRAM traffic per launch from the committed ncu capture of the variant family in use
     prof = f"ncu_{kernel}.txt"
-    if args.workload == "anyhit" and tv in (6, 7, 9, 10, 11, 12):  # unit rounds, leaf records out of L1
+    if args.workload == "anyhit" and tv in (6, 7, 9, 10, 11):  # unit rounds, leaf records out of L1
         prof = "ncu_trace_unit_stream.txt"
     traffic = _ncu_traffic(prof)
     torch.cuda.synchronize()

@@ -96,12 +96,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_batch_gather(
                 lux = __ldg(d->luxel_off + f) + (int64_t)iv * fr.nu + iu;
                 float px, py, pz;
                 luxel_sample(fr, lux, iu, iv, k, ss, seed, px, py, pz);
-                gather_point<kSkyTrace, kOptPacked>(scene, d->lights, d->nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z,
+                gather_point<kSkyTrace>(scene, d->lights, d->nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z,
                              r, g, b, rays);
                 lux_out = d->out_rgb;
             } else {
                 const float *p = d->ppts + 3 * local, *n = d->pnrm + 3 * local;
-                gather_point<kSkyTrace, kOptPacked>(scene, d->lights, d->nl, __ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(n),
+                gather_point<kSkyTrace>(scene, d->lights, d->nl, __ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(n),
                              __ldg(n + 1), __ldg(n + 2), r, g, b, rays);
                 float *o = d->pout + 3 * local;
                 o[0] = r;

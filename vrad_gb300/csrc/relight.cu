@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_relight_gather(
             const int64_t gsamp = lux * ss + kk;
             float px, py, pz;
             luxel_sample(fr, lux, iu, iv, kk, ss, seed, px, py, pz);
-            gather_point<SKY, kOptPacked>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g,
+            gather_point<SKY>(s, lights, nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z, r, g,
                               b, rays, sky_lux + gsamp * sky_slots, vis_lux + gsamp * vis_words, edited);
         } else if (gi < total) {
             const int64_t li = gi - nsamp;
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_relight_gather(
                 leaf = __ldg(list.leaf_beg + k) + (li - __ldg(list.leaf_off + k));
             }
             const float *p = ppts + 3 * leaf, *n = pnrm + 3 * leaf;
-            gather_point<SKY, kOptPacked>(s, lights, nl, __ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(n), __ldg(n + 1),
+            gather_point<SKY>(s, lights, nl, __ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(n), __ldg(n + 1),
                               __ldg(n + 2), r, g, b, rays, sky_pts + leaf * sky_slots,
                               vis_pts + leaf * vis_words, edited);
             pout[3 * leaf] = r;

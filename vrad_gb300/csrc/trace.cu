@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_closest(DevScene s, const fl
                 }
             }
         }
-        if (active && trace_step<kClosest, 1, kOptPacked>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
+        if (active && trace_step<kClosest, 1>(s, ray, rp, r0, r1, skip, 0.0f, st)) {
             active = false;
             hit[ri] = st.best;
             thit[ri] = st.best_t;
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kThreads) k_test_lines(DevScene s, const float
         float sx, sy, sz, ex, ey, ez;
         load3(start, i, sx, sy, sz);
         load3(stop, i, ex, ey, ez);
-        frac[i] = line_occluded<kOptPacked>(s, make_line(sx, sy, sz, ex, ey, ez), skip) ? 0.0f : 1.0f;
+        frac[i] = line_occluded(s, make_line(sx, sy, sz, ex, ey, ez), skip) ? 0.0f : 1.0f;
     }
 }
 
@@ -338,7 +338,7 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
 // lanes, with or without the vote, at the default or a 40-register cap,
 // leaf records kept out of L1 or not, top of the tree in shared memory or
-// not, packed triangle test, next plane loaded ahead).
+// not, next plane loaded ahead).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
@@ -346,8 +346,7 @@ const MaskKernel kMaskOcc[] = {
     k_trace_unit<false, 4, false, 1, kOptStream>, k_trace_unit<false, 8, false, 1, kOptStream>,
     k_trace_mask<false, 1, kOptStream>,
     k_trace_unit<false, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<false, 8, false, 1, kOptStream | kOptTop>,
-    k_trace_unit<false, 4, false, 1, kOptStream | kOptPacked>,
-    k_trace_unit<false, 4, false, 1, kOptStream | kOptPacked | kOptPipe>,
+    k_trace_unit<false, 4, false, 1, kOptStream | kOptPipe>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -356,10 +355,9 @@ const MaskKernel kMaskHit[] = {
     k_trace_unit<true, 4, false, 1, kOptStream>, k_trace_unit<true, 8, false, 1, kOptStream>,
     k_trace_mask<true, 1, kOptStream>,
     k_trace_unit<true, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<true, 8, false, 1, kOptStream | kOptTop>,
-    k_trace_unit<true, 4, false, 1, kOptStream | kOptPacked>,
-    k_trace_unit<true, 4, false, 1, kOptStream | kOptPacked | kOptPipe>,
+    k_trace_unit<true, 4, false, 1, kOptStream | kOptPipe>,
 };
-constexpr int kMaskVariants = 13;
+constexpr int kMaskVariants = 12;
 
 }  // namespace
 

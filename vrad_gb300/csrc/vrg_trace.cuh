@@ -32,7 +32,6 @@ constexpr int32_t kTraceIdSky = 0x01000000;
 // shared memory (stage_top).
 constexpr int kOptStream = 1;
 constexpr int kOptTop = 2;
-constexpr int kOptPacked = 4;  // triangle test on packed float32x2 instructions
 constexpr int kOptPipe = 8;    // unit rounds: the next triangle's plane loads during this test
 
 // Shared-memory copy of the scene's top table, for kernels walking with
@@ -217,19 +216,8 @@ template <int MODE, int OPT = 0>
 __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, float tmin, float tmax,
                                          int32_t skip, float any_limit, const float4 w0, size_t k,
                                          int32_t &best, float &best_t) {
-    float den, on;
-    if (OPT & kOptPacked) {
-        // (den, N.o) side by side: the same products and sums, in the same
-        // order, each lane of the pair rounded once
-        float2 m = __fmul2_rn(make_float2(w0.x, w0.x), make_float2(ray.dx, ray.ox));
-        m = __fadd2_rn(m, __fmul2_rn(make_float2(w0.y, w0.y), make_float2(ray.dy, ray.oy)));
-        m = __fadd2_rn(m, __fmul2_rn(make_float2(w0.z, w0.z), make_float2(ray.dz, ray.oz)));
-        den = m.x;
-        on = m.y;
-    } else {
-        den = dot3r(w0.x, w0.y, w0.z, ray.dx, ray.dy, ray.dz);
-        on = dot3r(w0.x, w0.y, w0.z, ray.ox, ray.oy, ray.oz);
-    }
+    const float den = dot3r(w0.x, w0.y, w0.z, ray.dx, ray.dy, ray.dz);
+    const float on = dot3r(w0.x, w0.y, w0.z, ray.ox, ray.oy, ray.oz);
     const float t = rdiv(rsub(w0.w, on), den);
     if (!(t >= tmin && t < tmax)) return false;
     if (MODE != kAny && !(t <= best_t)) return false;
@@ -245,20 +233,10 @@ __device__ __forceinline__ bool tri_test(const DevScene &s, const Ray &ray, floa
     const float d0 = drop == 0 ? ray.dy : (drop == 1 ? ray.dz : ray.dx);
     const float d1 = drop == 0 ? ray.dz : (drop == 1 ? ray.dx : ray.dy);
     // edge words: w1 = (e0, e3, e1, e4), w2 = (e2, e5, id, index << 2 | drop)
-    float b0, b1;
-    if (OPT & kOptPacked) {
-        const float2 h = __fadd2_rn(make_float2(o0, o1), __fmul2_rn(make_float2(t, t), make_float2(d0, d1)));
-        const float2 b = __fadd2_rn(__fadd2_rn(__fmul2_rn(make_float2(w1.x, w1.y), make_float2(h.x, h.x)),
-                                               __fmul2_rn(make_float2(w1.z, w1.w), make_float2(h.y, h.y))),
-                                    make_float2(w2.x, w2.y));
-        b0 = b.x;
-        b1 = b.y;
-    } else {
-        const float h0 = radd(o0, rmul(t, d0));
-        const float h1 = radd(o1, rmul(t, d1));
-        b0 = radd(radd(rmul(w1.x, h0), rmul(w1.z, h1)), w2.x);
-        b1 = radd(radd(rmul(w1.y, h0), rmul(w1.w, h1)), w2.y);
-    }
+    const float h0 = radd(o0, rmul(t, d0));
+    const float h1 = radd(o1, rmul(t, d1));
+    const float b0 = radd(radd(rmul(w1.x, h0), rmul(w1.z, h1)), w2.x);
+    const float b1 = radd(radd(rmul(w1.y, h0), rmul(w1.w, h1)), w2.y);
     const float b2 = rsub(rsub(1.0f, b0), b1);
     if (b0 >= 0.0f && b1 >= 0.0f && b2 >= 0.0f) {
         const int32_t ti = (int32_t)(idx_drop >> 2);
