@@ -314,11 +314,14 @@ typedef struct vrg_light_edit {
 typedef struct vrg_server vrg_server;
 
 /* Bake a scene (as vrg_env_bake) and keep, per luxel sample and leaf point,
- * the multiplier of each sky-type light, so that later light edits re-trace
- * only the edited point and spot lights.  Checks free device memory first
- * (VRG_ERR_NOMEM when the scene does not fit with 1 GiB to spare). */
+ * the multiplier of each sky-type light and one visibility bit per light, so
+ * that later light edits re-trace only the edited lights.  Admission: checks
+ * free device memory first (VRG_ERR_NOMEM when the scene's relight state does
+ * not fit with the context's HBM reserve to spare). */
 int vrg_env_relight_prepare(vrg_env *env, int32_t supersamples, uint64_t seed,
                             int32_t max_bounces, float rel_tol);
+/* Device memory that admission keeps free for other work (default 1 GiB). */
+int vrg_ctx_set_hbm_reserve(vrg_ctx *ctx, uint64_t bytes);
 /* Apply light edits and update the scene: luxels and leaf points of the faces
  * within the old or new radius of an edited light are re-gathered (the same
  * values a full gather would give), then the bounce restarts from the

@@ -122,3 +122,22 @@ def test_sky_light_geometry_edit_rejected(gpu_ctx):
     bad = make_light(3, (0, 0, 0), (1.0, 1.0, 1.0), (0.0, 0.0, -1.0))  # turns into a sun
     with pytest.raises(VrgError, match="unsupported"):
         env.relight([(sky, bad)])
+
+
+def test_admission_refuses_when_reserve_cannot_be_kept(gpu_ctx):
+    # admission keeps the context's HBM reserve free: asking for more than the
+    # GPU has turns the scene away with VRG_ERR_NOMEM, and the scene is
+    # admitted once the reserve is back to normal
+    from vrad_gb300._lib import VrgError
+
+    lit, env, nl = _scene(gpu_ctx, 91, 24)
+    gpu_ctx.set_hbm_reserve(1 << 60)
+    try:
+        with pytest.raises(VrgError, match="out of memory"):
+            env.relight_prepare(4, 1, 20, 1e-3)
+        with pytest.raises(VrgError, match="call out of order"):
+            env.relight([], max_iters=4, rel_tol=1e-3)
+    finally:
+        gpu_ctx.set_hbm_reserve(1 << 30)
+    env.relight_prepare(4, 1, 20, 1e-3)
+    env.relight([], max_iters=4, rel_tol=1e-3)

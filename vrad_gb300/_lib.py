@@ -37,6 +37,7 @@ SIGNATURES = {
     "vrg_ctx_autotune_choice": (C.c_int, [P, C.c_char_p, P, P, I32]),
     "vrg_ctx_autotune_save": (C.c_int, [P, C.c_char_p]),
     "vrg_ctx_autotune_load": (C.c_int, [P, C.c_char_p]),
+    "vrg_ctx_set_hbm_reserve": (C.c_int, [P, U64]),
     "vrg_env_create": (C.c_int, [P, P]),
     "vrg_env_destroy": (None, [P]),
     "vrg_env_add_triangle": (C.c_int, [P, I32, P, P, P, P, C.c_uint16, I32]),

@@ -432,7 +432,12 @@ int relight_prepare(vrg_env *env, int32_t ss, uint64_t seed, int32_t max_bounces
                         16 * 4 * (size_t)nl + 12 * (size_t)nl;
     size_t free_b = 0, total_b = 0;
     VRG_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
-    if (need + ((size_t)1 << 30) > free_b)
+    uint64_t reserve;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        reserve = ctx->hbm_reserve;
+    }
+    if ((uint64_t)need > (uint64_t)free_b || (uint64_t)free_b - (uint64_t)need < reserve)
         return fail(ctx, VRG_ERR_NOMEM, "not enough free device memory to admit this scene for relighting");
     relight_release(env);  // loop graphs point into buffers that may move below
     VRG_CUDA(ctx, env->d_bake_rgb.reserve(12 * (size_t)std::max<int64_t>(nlux, 1)));
@@ -850,6 +855,13 @@ int vrg_env_relight_prepare(vrg_env *env, int32_t supersamples, uint64_t seed, i
     if (!env) return VRG_ERR_INVALID;
     std::lock_guard<std::mutex> lk(env->mu);
     return relight_prepare(env, supersamples, seed, max_bounces, rel_tol);
+}
+
+int vrg_ctx_set_hbm_reserve(vrg_ctx *ctx, uint64_t bytes) {
+    if (!ctx) return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->hbm_reserve = bytes;
+    return VRG_OK;
 }
 
 int vrg_env_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, int32_t max_iters, float rel_tol,

@@ -80,6 +80,7 @@ struct vrg_ctx {
     std::vector<cudaEvent_t> event_pool;
     int64_t launches = 0;
     bool autotune = true;
+    uint64_t hbm_reserve = (uint64_t)1 << 30;  // kept free when admitting a relight scene
     std::map<std::string, int> tuned;                   // bucket key -> variant
     std::map<std::string, std::vector<double>> tune_ms;  // bucket key -> variant times
 };

@@ -85,6 +85,10 @@ class Context:
     def launch_count(self) -> int:
         return int(self.lib.vrg_ctx_launch_count(self.h))
 
+    def set_hbm_reserve(self, nbytes: int):
+        """Device memory that relight admission keeps free (default 1 GiB)."""
+        check(self.lib.vrg_ctx_set_hbm_reserve(self.h, int(nbytes)), self.h, "set_hbm_reserve")
+
     def set_autotune(self, on: bool):
         check(self.lib.vrg_ctx_set_autotune(self.h, int(on)), self.h, "set_autotune")
 
