@@ -337,14 +337,20 @@ def run_gpu(args, rank, world, local_rank):
         m, st = pyoracle.Scene.occlusion_mask(s, sc.starts, sc.stops, threads=threads, stats=True)
         dt = time.perf_counter() - t0
         nodes, tris = st[:, 0].mean(), st[:, 1].mean()
-        bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
+        # per line: end points, mask bit, and per node / per triangle test the
+        # 8-byte node, the 48-byte record and its 4-byte TriangleIndexList entry
+        bytes_per_unit = 24 + 1 / 8 + 8 * nodes + (48 + 4) * tris
         cpu = {"value": round(n / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
                "kind": "port", "sample": f"all {n} lines"}
     else:
         cpu_faces = min(CPU_SAMPLE_FACES, lit.n_faces)
         rays_cpu, dt, st = _cpu_baseline(lit, cpu_faces, threads)
         nodes, tris = st[1] / st[0], st[2] / st[0]
-        bytes_per_unit = 8 * nodes + 48 * tris + (80 + 3) / (units / (4 * nlux))
+        # per shadow line: nodes, records and index entries as above, plus the
+        # sample's position and normal (24 B) and its share of the RGB output
+        # (12 B per luxel of 4 samples), spread over the sample's lines
+        rays_per_sample = units / (4 * nlux)
+        bytes_per_unit = 8 * nodes + (48 + 4) * tris + (24 + 12 / 4) / rays_per_sample
         cpu = {"value": round(rays_cpu / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
                "kind": "port",
                "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
@@ -364,6 +370,9 @@ def run_gpu(args, rank, world, local_rank):
             "peak_kind": f"{peak_kind} HBM copy",
             "kernel": kernel, "kernel_ms": round(avg_ms, 4),
             "bytes_per_ray": round(bytes_per_unit, 2),
+            "bytes_model": "8 per kd node + (48 record + 4 index) per triangle test, means of the "
+                           "oracle's walk over the same lines" + (" + 24 end points + 1/8 mask"
+                           if args.workload == "anyhit" else " + sample position, normal and RGB share"),
             "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
             "l2_read_gbs_measured": round(l2, 1) if l2 else None,
             "l2_frac": round(achieved / l2, 4) if l2 else None, "traffic_source": f"profiles/{prof}"}
@@ -375,6 +384,8 @@ def run_gpu(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 box rooms)",
         "config": {"workload": workload, "rays_per_step": units,
+                   **({} if args.workload == "anyhit" else
+                      {"luxel_samples_per_s_M": round(4 * nlux * args.steps * world / (total_ms * 1e-3) / 1e6, 3)}),
                    "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",
                    "autotune": {"bucket": tkey, "variant": tv,
                                 "variant_ms": [round(x, 4) for x in tms]}},
