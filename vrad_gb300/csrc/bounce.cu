@@ -7,10 +7,12 @@
 //   per bounce: add_i = sum_j w_ij emit_j ; total += add ; emit = refl * add
 //   delta = sum |add|_1 / sum |total|_1 ; stop after the bounce whose delta
 //   is below the tolerance, or after max_bounces.
-// Each bounce is one SpMV kernel plus one single-block reduction; a CUDA
-// graph holds several bounces and the kernels turn into no-ops once the
-// device-side control block says the loop is done.
+// Each bounce is one SpMV kernel plus one single-block reduction; the loop
+// is a CUDA graph whose conditional while node repeats a body of two bounces
+// until the reduce kernel, reading the device-side control block, clears
+// the condition.
 #include <algorithm>
+#include <memory>
 
 #include "vrg_internal.h"
 #include "vrg_spmv.cuh"
@@ -96,8 +98,14 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bounce_spmv(
 }
 
 // Sums the block partials in a fixed order and advances the control block.
-__global__ void k_bounce_reduce(BounceControl *ctl, const double *__restrict__ partials, int nblocks) {
-    if (*(volatile int32_t *)&ctl->done) return;
+// Inside the loop graph (in_loop) thread 0 also sets the loop's condition:
+// the while node runs its body again only while the loop is not done.
+__global__ void k_bounce_reduce(BounceControl *ctl, const double *__restrict__ partials, int nblocks,
+                                int in_loop, cudaGraphConditionalHandle loop) {
+    if (*(volatile int32_t *)&ctl->done) {
+        if (in_loop && threadIdx.x == 0) cudaGraphSetConditional(loop, 0u);
+        return;
+    }
     __shared__ double sa[256], st[256];
     double a = 0.0, t = 0.0;
     for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
@@ -118,11 +126,27 @@ __global__ void k_bounce_reduce(BounceControl *ctl, const double *__restrict__ p
         const float delta = st[0] > 0.0 ? (float)(sa[0] / st[0]) : 0.0f;
         ctl->last_delta = delta;
         ctl->iters += 1;
-        if (delta < ctl->tol || ctl->iters >= ctl->max_iters) ctl->done = 1;
+        const int done = delta < ctl->tol || ctl->iters >= ctl->max_iters;
+        if (done) ctl->done = 1;
+        if (in_loop) cudaGraphSetConditional(loop, done ? 0u : 1u);
     }
 }
 
 }  // namespace
+
+// The bounce loop of a scene as an executable graph (see run_bounce).
+struct BounceGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void *> key;  // the buffers, sizes and variant it was built on
+    ~BounceGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+void bounce_release(vrg_env *env) {
+    delete env->bounce_graph;
+    env->bounce_graph = nullptr;
+}
 
 int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounces, float *delta) {
     vrg_ctx *ctx = env->ctx;
@@ -185,7 +209,7 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
         if (e != cudaSuccess) return e;
         cudaEvent_t ev2 = nullptr;
         timing_begin(ctx, "bounce_reduce", &ev2);
-        k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, env->d_partials.as<double>(), nblocks);
+        k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, env->d_partials.as<double>(), nblocks, 0, 0);
         e = cudaGetLastError();
         timing_end(ctx, "bounce_reduce", ev2);
         return e;
@@ -193,8 +217,9 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
 
     BounceControl h{};
     int32_t launched = 0;
-    // With timing on, bounces launch one by one so each kernel gets events;
-    // otherwise a CUDA graph of kGraphBounces bounces is replayed.
+    // With timing on, bounces launch one by one so each kernel gets events
+    // (and the host checks the control block every kGraphBounces); otherwise
+    // the whole loop is one launch of the scene's loop graph.
     if (ctx->timing) {
         while (launched < max_bounces) {
             VRG_CUDA(ctx, one_bounce((launched & 1) ? e1 : e0, (launched & 1) ? e0 : e1));
@@ -206,33 +231,49 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
             }
         }
     } else if (max_bounces > 0) {
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        cudaStream_t cs = ctx->stream;
-        VRG_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        cudaError_t ce = cudaSuccess;
-        for (int b = 0; b < kGraphBounces && ce == cudaSuccess; b++) ce = one_bounce((b & 1) ? e1 : e0, (b & 1) ? e0 : e1);
-        cudaError_t ee = cudaStreamEndCapture(cs, &graph);
-        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "bounce capture");
-        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "cudaStreamEndCapture");
-        VRG_CUDA(ctx, cudaGraphInstantiate(&exec, graph, 0));
-        cudaGraphDestroy(graph);
-        while (launched < max_bounces) {
-            cudaError_t le = cudaGraphLaunch(exec, cs);
-            if (le != cudaSuccess) {
-                cudaGraphExecDestroy(exec);
-                return cuda_fail(ctx, le, "cudaGraphLaunch");
+        // the loop as a graph with a conditional while node (body: two
+        // bounces), kept on the scene and rebuilt only when a buffer it
+        // points into, the size or the SpMV variant changes
+        const std::vector<const void *> key = {e0, env->d_total.ptr, env->d_row_ptr.ptr, env->d_col.ptr,
+                                               env->d_weight.ptr, env->d_leaf_info.ptr, ctl,
+                                               env->d_partials.ptr, reinterpret_cast<const void *>((intptr_t)n),
+                                               reinterpret_cast<const void *>((intptr_t)nblocks),
+                                               reinterpret_cast<const void *>((intptr_t)var)};
+        if (!env->bounce_graph || env->bounce_graph->key != key) {
+            bounce_release(env);
+            std::unique_ptr<BounceGraph> bg(new BounceGraph);
+            cudaGraph_t g = nullptr;
+            VRG_CUDA(ctx, cudaGraphCreate(&g, 0));
+            cudaGraphConditionalHandle hc = 0;
+            cudaError_t e = cudaGraphConditionalHandleCreate(&hc, g, 1u, cudaGraphCondAssignDefault);
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = hc;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t wn = nullptr;
+            if (e == cudaSuccess) e = cudaGraphAddNode(&wn, g, nullptr, nullptr, 0, &cp);
+            if (e == cudaSuccess)
+                e = cudaStreamBeginCaptureToGraph(ctx->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                cudaError_t le = spmv(var, e0, e1);
+                k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, env->d_partials.as<double>(), nblocks, 1, hc);
+                if (le == cudaSuccess) le = cudaGetLastError();
+                if (le == cudaSuccess) le = spmv(var, e1, e0);
+                k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, env->d_partials.as<double>(), nblocks, 1, hc);
+                if (le == cudaSuccess) le = cudaGetLastError();
+                cudaGraph_t captured = nullptr;
+                e = cudaStreamEndCapture(ctx->stream, &captured);
+                if (e == cudaSuccess) e = le;
             }
-            launched += kGraphBounces;
-            cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, cs);
-            cudaError_t se = cudaStreamSynchronize(cs);
-            if (se != cudaSuccess) {
-                cudaGraphExecDestroy(exec);
-                return cuda_fail(ctx, se, "bounce graph");
-            }
-            if (h.done) break;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&bg->exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "bounce loop graph");
+            bg->key = key;
+            env->bounce_graph = bg.release();
         }
-        cudaGraphExecDestroy(exec);
+        VRG_CUDA(ctx, cudaGraphLaunch(env->bounce_graph->exec, ctx->stream));
     }
     VRG_CUDA(ctx, cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -346,7 +387,7 @@ extern "C" int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, f
             env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), in, out, total,
             env->d_leaf_info.as<LeafInfo>(), n, ctl, partials);
         VRG_CUDA(ctx, cudaGetLastError());
-        k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, partials, nblocks);
+        k_bounce_reduce<<<1, 256, 0, ctx->stream>>>(ctl, partials, nblocks, 0, 0);
         VRG_CUDA(ctx, cudaGetLastError());
         count_launch(ctx);
         count_launch(ctx);

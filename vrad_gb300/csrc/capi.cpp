@@ -233,6 +233,7 @@ void vrg_env_destroy(vrg_env *env) {
     cudaSetDevice(env->ctx->device);
     cudaStreamSynchronize(env->ctx->stream);
     relight_release(env);
+    bounce_release(env);
     delete env;
 }
 

@@ -53,6 +53,7 @@ struct DevBuf {
 };
 
 struct RelightState;  // relight.cu: serial scratch and loop graphs of a scene
+struct BounceGraph;   // bounce.cu: the scene's bounce loop as a graph
 
 struct KernelStat {
     double ms = 0.0;
@@ -160,6 +161,7 @@ struct vrg_env {
     vrg::DevBuf d_sky_lux, d_sky_pts, d_emit0, d_x;
     vrg::DevBuf d_vis_lux, d_vis_pts;       // point/spot shadow-line bits per sample / point
     vrg::RelightState *relight = nullptr;   // owned; freed by relight_release
+    vrg::BounceGraph *bounce_graph = nullptr;  // owned; freed by bounce_release
     std::vector<float> face_lo, face_hi;      // face bounds (3 floats each)
     std::vector<int32_t> face_leaf_begin;     // leaves of face f: [begin[f], begin[f+1])
 
@@ -227,5 +229,6 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k);
 int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounces,
                float *delta);
 void relight_release(vrg_env *env);
+void bounce_release(vrg_env *env);
 
 }  // namespace vrg
