@@ -2,9 +2,11 @@
  * vrad_oracle.h -- CPU oracle for the VRAD radiosity hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
- * algorithm, used by tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg as the checker.  The product library never links, loads or
- * calls it.
+ * algorithm, which tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg compare the library against.  The product library never
+ * links, loads or calls it.  Parity with the reference itself is unpinned:
+ * the reference's path cannot be built or run, and its tests hold no golden
+ * vectors for it; known-answer tests pin this restatement instead.
  *
  * Reference files restated (paths inside the reference project):
  *   raytracer/environment.go:41-138,181-403   triangle soup, SAH kd builder
