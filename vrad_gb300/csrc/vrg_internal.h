@@ -162,7 +162,7 @@ struct vrg_env {
     vrg::DevBuf d_vis_lux, d_vis_pts;       // point/spot shadow-line bits per sample / point
     vrg::RelightState *relight = nullptr;   // owned; freed by relight_release
     vrg::BounceGraph *bounce_graph = nullptr;  // owned; freed by bounce_release
-    std::vector<float> face_lo, face_hi;      // face bounds (3 floats each)
+    std::vector<float> face_mid, face_ext;      // face centres / padded half extents, axis-major ([a * nfaces + f])
     std::vector<int32_t> face_leaf_begin;     // leaves of face f: [begin[f], begin[f+1])
 
     // scratch for host-buffer entry points
