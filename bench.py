@@ -608,11 +608,9 @@ def run_serve(args, local_rank):
             reqs.append((s, edit_array(edits), len(edits)))
         return reqs
 
-    def run(slots, rate, reqs):
+    def run(slots, arrivals, reqs):
         srv = Server(ctx, slots=slots, max_iters=32, rel_tol=1e-3)
         ids = [srv.add_scene(env) for env in envs]
-        gaps = rng.exponential(1.0 / rate, len(reqs))
-        arrivals = np.cumsum(gaps)
         tickets = []
         t_start = time.perf_counter()
         for (s, arr, n), ta in zip(reqs, arrivals):
@@ -636,12 +634,15 @@ def run_serve(args, local_rank):
 
     # warm-up on both paths
     warm = make_requests()[:32]
-    run(8, 1000.0, warm)
-    run(1, 1000.0, warm)
+    warm_arr = np.cumsum(rng.exponential(1.0 / 1000.0, len(warm)))
+    run(8, warm_arr, warm)
+    run(1, warm_arr, warm)
     table = {}
     for rate in rates:
+        # one request stream per rate, the same requests at the same times on both paths
         reqs = make_requests()
-        table[str(int(rate))] = {"served": run(8, rate, reqs), "serial": run(1, rate, reqs)}
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+        table[str(int(rate))] = {"served": run(8, arrivals, reqs), "serial": run(1, arrivals, reqs)}
     top = table[str(int(rates[-1]))]
     line = {
         "metric": "relight p50/p99 ms and bakes/s (served vs plain serial)",

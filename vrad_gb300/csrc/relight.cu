@@ -331,9 +331,8 @@ int spmv_blocks(const vrg_ctx *ctx) {
 
 // Per-slot device scratch of a relight request.
 struct RelightScratch {
-    DevBuf buf;  // [ctl | counters | digest | partials | offsets | face list | edited mask]
+    DevBuf buf;  // [unused | counters | digest | digest partials | offsets | face list | edited mask]
     size_t cap_faces = 0, cap_words = 0;
-    RelightCtl *ctl = nullptr;
     unsigned long long *work = nullptr, *rays = nullptr;
     double *digest = nullptr, *partials = nullptr;
     int32_t *faces = nullptr, *leaf_beg = nullptr;
@@ -348,7 +347,6 @@ struct RelightScratch {
         const size_t bytes = head + (nfaces + 1) * (4 + 4 + 8 + 8) + 4 * nwords + 256;
         VRG_CUDA(ctx, buf.reserve(bytes));
         char *p = buf.as<char>();
-        ctl = reinterpret_cast<RelightCtl *>(p);
         work = reinterpret_cast<unsigned long long *>(p + 64);
         rays = work + 1;
         digest = reinterpret_cast<double *>(p + 128);
@@ -399,11 +397,25 @@ struct LoopGraph {
 };
 
 // Relight state a scene keeps between requests: the serial entry point's
-// scratch and staging buffer, and the loop graphs built for each scratch.
+// scratch and staging buffer, the bounce loop's control block and partial
+// sums, and the loop graph built on them.  Requests on one scene never run
+// at the same time (the server keeps them in order), so one control block
+// and one graph serve every slot.
 struct RelightState {
     RelightScratch sc;
     HostStage stage;
-    std::map<const RelightScratch *, std::unique_ptr<LoopGraph>> loops;
+    DevBuf loop_buf;  // [RelightCtl | 2 doubles per SpMV block]
+    RelightCtl *ctl = nullptr;
+    double *partials = nullptr;
+    std::unique_ptr<LoopGraph> loop;
+
+    int reserve_loop(vrg_ctx *ctx) {
+        if (ctl) return VRG_OK;
+        VRG_CUDA(ctx, loop_buf.reserve(256 + 2 * 8 * (size_t)kRelightMaxBlocks));
+        ctl = loop_buf.as<RelightCtl>();
+        partials = reinterpret_cast<double *>(loop_buf.as<char>() + 256);
+        return VRG_OK;
+    }
 };
 
 void relight_release(vrg_env *env) {
@@ -605,18 +617,21 @@ RelightState &relight_state(vrg_env *env) {
     return *env->relight;
 }
 
-// The loop graph of (env, sc), built on first use and rebuilt when a buffer
-// it points into has moved.
-int loop_graph(vrg_env *env, RelightScratch &sc, cudaStream_t st, int sblocks, cudaGraphExec_t *out) {
+// The scene's loop graph, built on first use and rebuilt when a buffer it
+// points into has moved.
+int loop_graph(vrg_env *env, cudaStream_t st, int sblocks, cudaGraphExec_t *out) {
     vrg_ctx *ctx = env->ctx;
+    RelightState &rs = relight_state(env);
+    int rc = rs.reserve_loop(ctx);
+    if (rc != VRG_OK) return rc;
     const int64_t n = (int64_t)env->patches.leaf_patch.size();
     float4 *B = env->d_total.as<float4>(), *emit = env->d_emit0.as<float4>();
     float4 *x0 = env->d_x.as<float4>(), *x1 = x0 + std::max<int64_t>(n, 1);
     const std::vector<const void *> key = {x0, B, emit, env->d_row_ptr.ptr, env->d_col.ptr, env->d_weight.ptr,
-                                           env->d_leaf_info.ptr, sc.ctl, sc.partials,
+                                           env->d_leaf_info.ptr, rs.ctl, rs.partials,
                                            reinterpret_cast<const void *>((intptr_t)n),
                                            reinterpret_cast<const void *>((intptr_t)sblocks)};
-    std::unique_ptr<LoopGraph> &slot = relight_state(env).loops[&sc];
+    std::unique_ptr<LoopGraph> &slot = rs.loop;
     if (slot && slot->key == key) {
         *out = slot->exec;
         return VRG_OK;
@@ -640,10 +655,10 @@ int loop_graph(vrg_env *env, RelightScratch &sc, cudaStream_t st, int sblocks, c
         const int64_t *rp = env->d_row_ptr.as<int64_t>();
         const int32_t *col = env->d_col.as<int32_t>();
         const float *w = env->d_weight.as<float>();
-        k_relight_spmv<<<sblocks, kSpmvThreads, 0, st>>>(rp, col, w, x0, x1, B, emit, info, n, sc.ctl, sc.partials);
-        k_relight_reduce<<<1, 256, 0, st>>>(sc.ctl, sc.partials, sblocks, 1, h);
-        k_relight_spmv<<<sblocks, kSpmvThreads, 0, st>>>(rp, col, w, x1, x0, B, emit, info, n, sc.ctl, sc.partials);
-        k_relight_reduce<<<1, 256, 0, st>>>(sc.ctl, sc.partials, sblocks, 1, h);
+        k_relight_spmv<<<sblocks, kSpmvThreads, 0, st>>>(rp, col, w, x0, x1, B, emit, info, n, rs.ctl, rs.partials);
+        k_relight_reduce<<<1, 256, 0, st>>>(rs.ctl, rs.partials, sblocks, 1, h);
+        k_relight_spmv<<<sblocks, kSpmvThreads, 0, st>>>(rp, col, w, x1, x0, B, emit, info, n, rs.ctl, rs.partials);
+        k_relight_reduce<<<1, 256, 0, st>>>(rs.ctl, rs.partials, sblocks, 1, h);
         const cudaError_t le = cudaGetLastError();
         cudaGraph_t captured = nullptr;
         e = cudaStreamEndCapture(st, &captured);
@@ -717,12 +732,15 @@ int issue_relight(vrg_env *env, const RelightPlan &p, int32_t max_iters, float t
     float4 *B = env->d_total.as<float4>(), *emit = env->d_emit0.as<float4>();
     float4 *x0 = env->d_x.as<float4>(), *x1 = x0 + std::max<int64_t>(n, 1);
     const int ib = (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), (int64_t)ctx->num_sms * 8);
+    RelightState &rs = relight_state(env);
+    rc = rs.reserve_loop(ctx);
+    if (rc != VRG_OK) return rc;
     k_relight_start<<<ib, 256, 0, st>>>(env->d_leaf_info.as<LeafInfo>(), env->d_leaf_direct.as<float>(), B, emit,
-                                        x0, n, sc.ctl, max_iters, tol);
+                                        x0, n, rs.ctl, max_iters, tol);
     VRG_CUDA(ctx, cudaGetLastError());
     // the loop runs on the device until the control block is done
     cudaGraphExec_t loop = nullptr;
-    rc = loop_graph(env, sc, st, spmv_blocks(ctx), &loop);
+    rc = loop_graph(env, st, spmv_blocks(ctx), &loop);
     if (rc != VRG_OK) return rc;
     VRG_CUDA(ctx, cudaGraphLaunch(loop, st));
     k_digest_partial<<<kDigestBlocks, 256, 0, st>>>(env->d_bake_rgb.as<float>(), 3 * env->luxel_offset.back(), B, n,
@@ -811,7 +829,8 @@ int start_slot(vrg_server *s, Slot &sl, Request *r) {
     if (rc != VRG_OK) return rc;
     env->lights = plan.table;
     char *res = static_cast<char *>(sl.result.ptr);
-    VRG_CUDA(s->ctx, cudaMemcpyAsync(res, sl.scratch.ctl, sizeof(RelightCtl), cudaMemcpyDeviceToHost, sl.stream));
+    VRG_CUDA(s->ctx, cudaMemcpyAsync(res, relight_state(env).ctl, sizeof(RelightCtl), cudaMemcpyDeviceToHost,
+                                     sl.stream));
     VRG_CUDA(s->ctx, cudaMemcpyAsync(res + 64, sl.scratch.digest, 16, cudaMemcpyDeviceToHost, sl.stream));
     VRG_CUDA(s->ctx, cudaMemcpyAsync(res + 128, sl.scratch.rays, 8, cudaMemcpyDeviceToHost, sl.stream));
     VRG_CUDA(s->ctx, cudaEventRecord(sl.done, sl.stream));
@@ -889,7 +908,7 @@ int vrg_env_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, int32_
     if (rc != VRG_OK) return rc;
     env->lights = plan.table;
     RelightCtl c;
-    VRG_CUDA(ctx, cudaMemcpyAsync(&c, sc.ctl, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+    VRG_CUDA(ctx, cudaMemcpyAsync(&c, rs.ctl, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
     VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (out_bounces) *out_bounces = c.iters;
     if (out_delta) *out_delta = c.last_delta;
