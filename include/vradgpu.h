@@ -333,7 +333,9 @@ int vrg_env_relight(vrg_env *env, const vrg_light_edit *edits, int32_t n, int32_
  * A worker thread admits pending requests into free slots as soon as they
  * free up; requests on different scenes overlap on the GPU, requests on the
  * same scene run in submission order.  A scene added to a server must only
- * be changed through it while the server lives. */
+ * be changed through it while the server lives: in particular it must not be
+ * relit with vrg_env_relight meanwhile, since both use the scene's one bounce
+ * control block and loop graph. */
 int vrg_server_create(vrg_ctx *ctx, int32_t slots, int32_t max_iters, float rel_tol,
                       vrg_server **out);
 void vrg_server_destroy(vrg_server *server);
