@@ -25,7 +25,8 @@
  *
  * Parity status: unpinned against the reference itself (it has no Go
  * toolchain here and no golden vectors for this path); pinned by the
- * known-answer tests in tests/test_oracle_kat.py.
+ * known-answer tests in tests/test_oracle_kat.py and, for the trace
+ * semantics, by float64 geometry in tests/golden/trace_geometry.npz.
  */
 #ifndef VRAD_ORACLE_H
 #define VRAD_ORACLE_H
