@@ -30,6 +30,7 @@ sys.path.insert(0, str(ROOT))
 
 SEED = 0
 CPU_SAMPLE_FACES = 1024  # bounded CPU baseline sample: faces [0, 1024) of 4,096
+STATS_SAMPLE_FACES = 256  # faces whose walk is counted for the byte model
 REF_FACES_PER_STEP = 256  # reference arm: faces per timed step
 
 
@@ -107,10 +108,15 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def _cpu_baseline(lit, faces, threads):
+def _cpu_baseline(lit, faces, threads, walk_tree=None):
+    """Oracle gather over faces [0, faces): shadow rays, seconds, walk stats.
+    walk_tree: walk that tree instead of the reference's (for counting the
+    device's node and triangle reads)."""
     from oracle import pyoracle
 
     s = pyoracle.Scene(lit.xyz, lit.ids)
+    if walk_tree is not None:
+        s.set_tree(*walk_tree)
     lights = pyoracle.make_lights(lit.lights)
     t0 = time.perf_counter()
     _, rays, st = pyoracle.gather_luxels(s, lights, len(lit.lights), lit, 0, faces, ss=4,
@@ -334,23 +340,28 @@ def run_gpu(args, rank, world, local_rank):
 
         s = pyoracle.Scene(sc.xyz, sc.ids)
         t0 = time.perf_counter()
-        m, st = pyoracle.Scene.occlusion_mask(s, sc.starts, sc.stops, threads=threads, stats=True)
+        m = pyoracle.Scene.occlusion_mask(s, sc.starts, sc.stops, threads=threads)
         dt = time.perf_counter() - t0
+        # node and triangle counts of the walk the device does (its own tree)
+        s.set_tree(*env.walk_tree()[:3])
+        _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
         nodes, tris = st[:, 0].mean(), st[:, 1].mean()
         # per line: end points, mask bit, and per node / per triangle test the
-        # 8-byte node, the 48-byte record and its 4-byte TriangleIndexList entry
-        bytes_per_unit = 24 + 1 / 8 + 8 * nodes + (48 + 4) * tris
+        # 8-byte node and the 48-byte leaf record
+        bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
         cpu = {"value": round(n / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
                "kind": "port", "sample": f"all {n} lines"}
     else:
         cpu_faces = min(CPU_SAMPLE_FACES, lit.n_faces)
-        rays_cpu, dt, st = _cpu_baseline(lit, cpu_faces, threads)
+        rays_cpu, dt, _ = _cpu_baseline(lit, cpu_faces, threads, None)
+        _, _, st = _cpu_baseline(lit, min(STATS_SAMPLE_FACES, lit.n_faces), threads,
+                                 env.walk_tree()[:3])
         nodes, tris = st[1] / st[0], st[2] / st[0]
-        # per shadow line: nodes, records and index entries as above, plus the
-        # sample's position and normal (24 B) and its share of the RGB output
-        # (12 B per luxel of 4 samples), spread over the sample's lines
+        # per shadow line: nodes and leaf records as above, plus the sample's
+        # position and normal (24 B) and its share of the RGB output (12 B per
+        # luxel of 4 samples), spread over the sample's lines
         rays_per_sample = units / (4 * nlux)
-        bytes_per_unit = 8 * nodes + (48 + 4) * tris + (24 + 12 / 4) / rays_per_sample
+        bytes_per_unit = 8 * nodes + 48 * tris + (24 + 12 / 4) / rays_per_sample
         cpu = {"value": round(rays_cpu / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
                "kind": "port",
                "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
@@ -370,8 +381,9 @@ def run_gpu(args, rank, world, local_rank):
             "peak_kind": f"{peak_kind} HBM copy",
             "kernel": kernel, "kernel_ms": round(avg_ms, 4),
             "bytes_per_ray": round(bytes_per_unit, 2),
-            "bytes_model": "8 per kd node + (48 record + 4 index) per triangle test, means of the "
-                           "oracle's walk over the same lines" + (" + 24 end points + 1/8 mask"
+            "bytes_model": "8 per kd node + 48 per triangle test (leaf-ordered records), means "
+                           "of the oracle's walk of the device's tree over the same lines" +
+                           (" + 24 end points + 1/8 mask"
                            if args.workload == "anyhit" else " + sample position, normal and RGB share"),
             "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
             "l2_read_gbs_measured": round(l2, 1) if l2 else None,

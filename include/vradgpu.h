@@ -140,14 +140,26 @@ int vrg_env_add_axis_aligned_rectangular_solid(vrg_env *env, int32_t id, const f
  * cmd/tasks/loadbsp/main.go:276,338. */
 int vrg_env_add_triangles(vrg_env *env, const float *xyz, const int32_t *ids, int64_t n);
 /* SetupAccelerationStructure (environment.go:119-138): SAH kd tree built on
- * the host with the reference's candidates, costs and partition order, then
- * the tree and intersection records are uploaded and stay resident. */
+ * the host with the reference's candidates, costs and partition order.  The
+ * device walks a second tree of the same format built with every candidate
+ * plane (the walk tree); it is uploaded with the intersection records and
+ * stays resident.  Both trees give the same answers: every query returns
+ * what testing every triangle would. */
 int vrg_env_setup_acceleration_structure(vrg_env *env);
 int64_t vrg_env_num_triangles(const vrg_env *env);
-/* Size of the built tree: nodes, triangle-index-list length, tree height. */
+/* Size of the reference's tree: nodes, triangle-index-list length, height. */
 int vrg_env_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height);
 /* OptimizedKDTree (children word, split float) and TriangleIndexList. */
 int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs);
+/* SAH costs of the walk tree (defaults 1, 1.5, 0.8, 28): a split costs
+ * traversal + intersection * (P_left * N_left + P_right * N_right), times
+ * empty_bonus when a side is empty; depth at most max_depth (< 32).  Only
+ * before vrg_env_setup_acceleration_structure. */
+int vrg_env_set_walk_tree_costs(vrg_env *env, float traversal, float intersection,
+                                float empty_bonus, int32_t max_depth);
+/* The walk tree, in the format of vrg_env_tree_info / vrg_env_get_tree. */
+int vrg_env_walk_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height);
+int vrg_env_get_walk_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs);
 /* GetTriangle (environment.go:422-424): the 48-byte TriIntersectData
  * (raytracer/cache/triangle/triintersectdata.go:3-22) of triangle `index`. */
 int vrg_env_get_triangle(const vrg_env *env, int64_t index, void *out48);

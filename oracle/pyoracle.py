@@ -108,6 +108,16 @@ class Scene:
         L.orc_scene_get_tree(C.c_void_p(self.h), _p(ch), _p(sp), _p(refs))
         return ch, sp, refs[:nr]
 
+    def set_tree(self, children, split, refs):
+        """Walk another tree of the same format (e.g. the library's walk tree)."""
+        ch = np.ascontiguousarray(children, np.uint32)
+        sp = np.ascontiguousarray(split, np.float32)
+        rf = np.ascontiguousarray(refs, np.int32)
+        rc = lib().orc_scene_set_tree(C.c_void_p(self.h), _p(ch), _p(sp), C.c_int64(ch.size),
+                                      _p(rf), C.c_int64(rf.size))
+        if rc != 0:
+            raise RuntimeError("orc_scene_set_tree failed")
+
     def tris(self):
         out = (OTri * max(self.n, 1))()
         lib().orc_scene_get_tris(C.c_void_p(self.h), out)

@@ -377,6 +377,36 @@ void orc_scene_get_tree(const orc_scene *s, uint32_t *children, float *split, in
     if (split) memcpy(split, s->split, sizeof(float) * (size_t)s->nnodes);
     if (refs) memcpy(refs, s->refs, sizeof(int32_t) * (size_t)s->nrefs);
 }
+/* Replaces the scene's tree with another of the same format (children word,
+ * split or leaf count, triangle index list), e.g. the library's walk tree,
+ * so that its walk can be checked against brute force and counted.  The
+ * walk visits at most one stacked subtree per level: depth < STACK_MAX. */
+int orc_scene_set_tree(orc_scene *s, const uint32_t *children, const float *split,
+                       int64_t nnodes, const int32_t *refs, int64_t nrefs) {
+    if (nnodes < 1) return -1;
+    uint32_t *c = malloc(sizeof(uint32_t) * (size_t)nnodes);
+    float *f = malloc(sizeof(float) * (size_t)nnodes);
+    int32_t *r = malloc(sizeof(int32_t) * (size_t)(nrefs > 0 ? nrefs : 1));
+    if (!c || !f || !r) {
+        free(c);
+        free(f);
+        free(r);
+        return -1;
+    }
+    memcpy(c, children, sizeof(uint32_t) * (size_t)nnodes);
+    memcpy(f, split, sizeof(float) * (size_t)nnodes);
+    if (nrefs > 0) memcpy(r, refs, sizeof(int32_t) * (size_t)nrefs);
+    free(s->children);
+    free(s->split);
+    free(s->refs);
+    s->children = c;
+    s->split = f;
+    s->refs = r;
+    s->nnodes = s->cap_nodes = nnodes;
+    s->nrefs = s->cap_refs = nrefs;
+    return 0;
+}
+
 void orc_scene_get_tris(const orc_scene *s, orc_tri *out) {
     memcpy(out, s->tris, sizeof(orc_tri) * (size_t)s->ntris);
 }

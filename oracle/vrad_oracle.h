@@ -83,6 +83,9 @@ int64_t orc_scene_num_nodes(const orc_scene *s);
 int64_t orc_scene_num_refs(const orc_scene *s);
 void orc_scene_get_tree(const orc_scene *s, uint32_t *children, float *split, int32_t *refs);
 void orc_scene_get_tris(const orc_scene *s, orc_tri *out);
+/* replace the tree (same format as orc_scene_get_tree); 0 on success */
+int orc_scene_set_tree(orc_scene *s, const uint32_t *children, const float *split,
+                       int64_t nnodes, const int32_t *refs, int64_t nrefs);
 void orc_scene_bounds(const orc_scene *s, float *bmin, float *bmax);
 int orc_scene_depth(const orc_scene *s);
 

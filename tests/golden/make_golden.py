@@ -56,15 +56,18 @@ def sha(*arrays) -> str:
 
 
 def geometry_scene(seed: int = 17, n_boxes: int = 96, n_lines: int = 2048):
-    """Room (ceiling sky) + boxes with their own ids, every fourth one sky;
-    half of the lines end inside a box so that most of them hit something."""
+    """Room (ceiling sky) + boxes with their own ids: every fourth one sky,
+    every fourth (offset 1) a static prop (TRACE_ID_STATICPROP | index), the
+    rest opaque; half of the lines end inside a box so that most of them hit
+    something."""
     soup = scenes.TriangleSoup()
     soup.add_box(scenes.TRACE_ID_OPAQUE, (0.0, 0.0, 0.0), (scenes.ROOM,) * 3,
                  ceiling_id=scenes.TRACE_ID_SKY)
     mins, maxs = scenes._random_boxes(scenes.Stream(seed, scenes.S_BOXES), n_boxes, 64.0, 512.0)
     box_id = []
     for b in range(n_boxes):
-        flag = scenes.TRACE_ID_SKY if b % 4 == 0 else scenes.TRACE_ID_OPAQUE
+        flag = (scenes.TRACE_ID_SKY, scenes.TRACE_ID_STATICPROP)[b % 4] if b % 4 < 2 \
+            else scenes.TRACE_ID_OPAQUE
         box_id.append(flag | (b << 1))
         soup.add_box(box_id[-1], mins[b], maxs[b])
     xyz, ids = soup.arrays()
@@ -144,8 +147,11 @@ def make_trace_geometry():
     xyz, ids, starts, stops = geometry_scene()
     frames = _tri_frames(xyz)
     hit0, t0, occ0 = _answer(frames, ids, starts, stops, -1)
-    # skip the id that is the closest hit of the most lines
+    # skip the static-prop id that is the closest hit of the most lines (so
+    # that TestLineDoesHitSky's staticPropToSkip can name it too)
     hit_ids, counts = np.unique(ids[hit0[hit0 >= 0]], return_counts=True)
+    prop = (hit_ids & scenes.TRACE_ID_STATICPROP) != 0
+    hit_ids, counts = hit_ids[prop], counts[prop]
     skip = int(hit_ids[np.argmax(counts)])
     hit1, t1, occ1 = _answer(frames, ids, starts, stops, skip)
     out = dict(xyz=xyz, ids=ids, starts=starts, stops=stops,

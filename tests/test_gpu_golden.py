@@ -35,7 +35,9 @@ def test_lines_match_float64_geometry(geom_env, geom, k):
     skip = int(g["skip_ids"][k])
     mask, hit, t = geom_env.occlusion_mask(g["starts"], g["stops"], skip_id=skip, closest=True)
     check_against_geometry(g, k, hit, t, mask=mask)
-    frac = geom_env.test_line_does_hit_sky(g["starts"], g["stops"], skip)
+    # testline.go:36 skips id TRACE_ID_STATICPROP | staticPropToSkip
+    prop = -1 if skip == -1 else skip & ~mg.scenes.TRACE_ID_STATICPROP
+    frac = geom_env.test_line_does_hit_sky(g["starts"], g["stops"], prop)
     check_against_geometry(g, k, hit, t, frac=frac)
     # the same segments as rays (unit direction, [0, len))
     d = (g["stops"] - g["starts"]).astype(np.float32)

@@ -50,6 +50,91 @@ def test_kd_tree_matches_oracle(oracle, host_ctx, which, anyhit_scene, lit_scene
     assert np.array_equal(env.triangle_records(), s.tri_records())
 
 
+def _walk_tree_scene(which, anyhit_scene, lit_scene):
+    rng = np.random.default_rng(11)
+    if which == "anyhit":
+        return anyhit_scene.xyz, anyhit_scene.ids, anyhit_scene.starts[:40000], \
+            anyhit_scene.stops[:40000]
+    if which == "lit":  # sky ceiling; lines from face points up and across
+        xyz, ids = lit_scene.xyz, lit_scene.ids
+        a = rng.uniform(1, 4095, (30000, 3)).astype(np.float32)
+        b = a + rng.normal(0, 1500, (30000, 3)).astype(np.float32)
+        b[::3, 2] = 4096.0 + 50.0  # through the sky ceiling
+        return xyz, ids, a, b.astype(np.float32)
+    # overlapping, non axis-aligned triangles and coplanar duplicates
+    c = rng.uniform(0, 1000, (3000, 1, 3))
+    xyz = (c + rng.normal(0, 30, (3000, 3, 3))).reshape(-1, 9).astype(np.float32)
+    xyz[1::7] = xyz[::7][: len(xyz[1::7])]
+    ids = np.full(3000, 0x02000000, np.int32)
+    a = rng.uniform(-50, 1050, (30000, 3)).astype(np.float32)
+    b = rng.uniform(-50, 1050, (30000, 3)).astype(np.float32)
+    return xyz, ids, a, b
+
+
+@pytest.mark.parametrize("which", ["anyhit", "lit", "random"])
+def test_walk_tree_gives_the_reference_trees_answers(oracle, host_ctx, which, anyhit_scene,
+                                                     lit_scene):
+    # the device walks its own tree; the oracle's walk over that tree must
+    # give the answers of the reference's tree and of brute force
+    xyz, ids, a, b = _walk_tree_scene(which, anyhit_scene, lit_scene)
+    env = _env(host_ctx, xyz, ids)
+    ch, sp, refs, height = env.walk_tree()
+    assert height < 32
+    assert np.array_equal(np.unique(refs), np.arange(len(ids)))  # every triangle in a leaf
+    ref = oracle.Scene(xyz, ids)
+    walk = oracle.Scene(xyz, ids)
+    walk.set_tree(ch, sp, refs)
+    m0, h0, t0 = ref.occlusion_mask(a, b, threads=16, closest=True)
+    m1, h1, t1 = walk.occlusion_mask(a, b, threads=16, closest=True)
+    assert np.array_equal(m0, m1) and np.array_equal(h0, h1) and bits_equal(t0, t1)
+    d = (b - a).astype(np.float32)
+    o = a[:4000]
+    hb, tb = ref.trace_closest(o, d[:4000], 0.0, 1.0, brute=True, threads=16)
+    hw, tw = walk.trace_closest(o, d[:4000], 0.0, 1.0, threads=16)
+    assert np.array_equal(hb, hw) and bits_equal(tb, tw)
+    assert np.array_equal(walk.test_lines(a, b, threads=16), ref.test_lines(a, b, threads=16))
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 7, 25])
+def test_walk_tree_small_and_degenerate(oracle, host_ctx, n):
+    rng = np.random.default_rng(n)
+    xyz = rng.uniform(0, 10, (n, 9)).astype(np.float32)
+    if n >= 3:
+        xyz[0, 2::3] = 1.0
+        xyz[1] = xyz[1, :3].tolist() * 3
+    ids = np.full(n, 0x02000000, np.int32)
+    env = _env(host_ctx, xyz, ids)
+    ch, sp, refs, height = env.walk_tree()
+    assert len(ch) >= 1 and height < 32
+    if n:
+        assert np.array_equal(np.unique(refs), np.arange(n))
+        walk = oracle.Scene(xyz, ids)
+        walk.set_tree(ch, sp, refs)
+        a = rng.uniform(-1, 11, (2000, 3)).astype(np.float32)
+        b = rng.uniform(-1, 11, (2000, 3)).astype(np.float32)
+        ref = oracle.Scene(xyz, ids)
+        _, h0, t0 = ref.occlusion_mask(a, b, threads=4, closest=True)
+        _, h1, t1 = walk.occlusion_mask(a, b, threads=4, closest=True)
+        assert np.array_equal(h0, h1) and bits_equal(t0, t1)
+
+
+def test_walk_tree_costs_are_checked(host_ctx, anyhit_scene):
+    from vrad_gb300._lib import VrgError
+    from vrad_gb300.environment import Environment
+
+    env = Environment(host_ctx)
+    with pytest.raises(VrgError):
+        env.set_walk_tree_costs(max_depth=32)
+    with pytest.raises(VrgError):
+        env.set_walk_tree_costs(empty_bonus=1.5)
+    env.set_walk_tree_costs(1.0, 1.5, 0.9, 20)
+    env.add_triangles(anyhit_scene.xyz[:600], anyhit_scene.ids[:600])
+    env.SetupAccelerationStructure()
+    assert env.walk_tree()[3] <= 20
+    with pytest.raises(VrgError):
+        env.set_walk_tree_costs()
+
+
 @pytest.mark.parametrize("n", [0, 1, 2, 3, 7, 25])
 def test_kd_tree_small_and_degenerate(oracle, host_ctx, n):
     rng = np.random.default_rng(n)

@@ -77,7 +77,8 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     const int64_t n = (int64_t)env->ids.size();
     if (n >= (int64_t)1 << 30) return fail(ctx, VRG_ERR_UNSUPPORTED, "more than 2^30 triangles");
     build_kd_tree(env->xyz, env->tree, env->min_bound, env->max_bound);
-    if (env->tree.height >= kStackMax)
+    build_walk_tree(env->xyz, env->min_bound, env->max_bound, env->walk_costs, env->walk_tree);
+    if (env->walk_tree.height >= kStackMax)
         return fail(ctx, VRG_ERR_UNSUPPORTED, "kd tree deeper than the traversal stack");
 
     env->tri_records.resize(n);
@@ -105,16 +106,17 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     }
     g.scale = scale;
 
-    // device upload: nodes (8 B), then in TriangleIndexList order the
+    // device upload of the walk tree: nodes (8 B), then in leaf order the
     // triangle planes (16 B each) followed by the edge parts (32 B each:
     // (e0, e3, e1, e4), (e2, e5, id, index << 2 | drop)), NTriangleID per
     // triangle
-    const size_t nn = env->tree.children.size(), nr = env->tree.refs.size();
+    const HostTree &wt = env->walk_tree;
+    const size_t nn = wt.children.size(), nr = wt.refs.size();
     std::vector<uint2> nodes(nn);
     for (size_t i = 0; i < nn; i++) {
         uint32_t sbits;
-        memcpy(&sbits, &env->tree.split[i], 4);
-        nodes[i] = make_uint2(env->tree.children[i], sbits);
+        memcpy(&sbits, &wt.split[i], 4);
+        nodes[i] = make_uint2(wt.children[i], sbits);
     }
     // top table: breadth-first from the root, a pair of children at a
     // time, while it fits; children words of nodes whose children made it
@@ -147,7 +149,7 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     const size_t nr1 = nr ? nr : 1;
     std::vector<float4> leaf(3 * nr1, make_float4(0, 0, 0, 0));
     for (size_t r = 0; r < nr; r++) {
-        const TriRecord &t = env->tri_records[env->tree.refs[r]];
+        const TriRecord &t = env->tri_records[wt.refs[r]];
         float id_bits, idx_bits;
         memcpy(&id_bits, &t.id, 4);
         memcpy(&idx_bits, &t.idx_drop, 4);
@@ -191,6 +193,37 @@ int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32
     if (children) memcpy(children, env->tree.children.data(), env->tree.children.size() * 4);
     if (split) memcpy(split, env->tree.split.data(), env->tree.split.size() * 4);
     if (refs) memcpy(refs, env->tree.refs.data(), env->tree.refs.size() * 4);
+    return VRG_OK;
+}
+
+int vrg_env_set_walk_tree_costs(vrg_env *env, float traversal, float intersection,
+                                float empty_bonus, int32_t max_depth) {
+    if (!env || !(traversal > 0.0f) || !(intersection > 0.0f) || !(empty_bonus > 0.0f) ||
+        !(empty_bonus <= 1.0f) || max_depth < 1 || max_depth >= kStackMax)
+        return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(env->mu);
+    if (env->built) return fail(env->ctx, VRG_ERR_STATE, "walk tree costs set after the build");
+    env->walk_costs.traversal = traversal;
+    env->walk_costs.intersection = intersection;
+    env->walk_costs.empty_bonus = empty_bonus;
+    env->walk_costs.max_depth = max_depth;
+    return VRG_OK;
+}
+
+int vrg_env_walk_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height) {
+    if (!env || !env->built) return VRG_ERR_STATE;
+    if (nodes) *nodes = (int64_t)env->walk_tree.children.size();
+    if (refs) *refs = (int64_t)env->walk_tree.refs.size();
+    if (height) *height = env->walk_tree.height;
+    return VRG_OK;
+}
+
+int vrg_env_get_walk_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs) {
+    if (!env || !env->built) return VRG_ERR_STATE;
+    const HostTree &t = env->walk_tree;
+    if (children) memcpy(children, t.children.data(), t.children.size() * 4);
+    if (split) memcpy(split, t.split.data(), t.split.size() * 4);
+    if (refs) memcpy(refs, t.refs.data(), t.refs.size() * 4);
     return VRG_OK;
 }
 

@@ -151,7 +151,162 @@ struct Builder {
     }
 };
 
+// The tree the device walks.  Any tree whose leaves hold every triangle
+// that touches their cell gives the walk the same answers (closest hit =
+// brute force, ties to the lower index), so the device is free to use a
+// better one than the reference's, whose SAH only tries the vertices of
+// every (1 + n/10)-th triangle.  This one evaluates every candidate plane:
+// the triangles' extents clamped to the node's box, swept in sorted order on
+// each axis (the event sweep of Wald & Havran, "On building fast kd-trees
+// for ray tracing, and on doing that in O(N log N)", 2006, here with a sort
+// per node).  Cost of a split = traversal + intersection * (P_L * N_L +
+// P_R * N_R) (P = surface-area ratio), times empty_bonus when one side is
+// empty; triangles lying in the plane go to the cheaper side.  A node
+// becomes a leaf when no split is cheaper than intersection * N, when it
+// holds one triangle, or at depth max_depth.  The node numbering (children
+// in adjacent pairs, left at the odd index) and the leaf format are those of
+// the reference's tree.
+struct WalkBuilder {
+    const float *xyz;
+    HostTree &tree;
+    WalkTreeCosts cost;
+    std::vector<float> lo[3], hi[3];
+
+    struct Event {
+        float p;
+        int kind;  // 0 ends here, 1 lies in the plane, 2 starts here
+    };
+
+    WalkBuilder(const float *x, int64_t n, HostTree &t, const WalkTreeCosts &c)
+        : xyz(x), tree(t), cost(c) {
+        for (int a = 0; a < 3; a++) {
+            lo[a].resize(n);
+            hi[a].resize(n);
+        }
+        for (int64_t i = 0; i < n; i++)
+            for (int a = 0; a < 3; a++) {
+                const float v0 = x[9 * i + a], v1 = x[9 * i + 3 + a], v2 = x[9 * i + 6 + a];
+                lo[a][i] = std::min(v0, std::min(v1, v2));
+                hi[a][i] = std::max(v0, std::max(v1, v2));
+            }
+    }
+
+    static double area(const float *mn, const float *mx) {
+        const double d0 = (double)mx[0] - mn[0], d1 = (double)mx[1] - mn[1],
+                     d2 = (double)mx[2] - mn[2];
+        return 2.0 * (d0 * d1 + d0 * d2 + d1 * d2);
+    }
+
+    void leaf(int node, const std::vector<int32_t> &list) {
+        tree.children[node] = kLeaf + ((uint32_t)tree.refs.size() << 2);
+        tree.split[node] = (float)list.size();
+        tree.refs.insert(tree.refs.end(), list.begin(), list.end());
+    }
+
+    void refine(int node, std::vector<int32_t> list, const float *mn, const float *mx, int level) {
+        tree.height = std::max(tree.height, level + 1);
+        const int n = (int)list.size();
+        if (n <= 1 || level + 1 >= cost.max_depth) {
+            leaf(node, list);
+            return;
+        }
+        const double sa = area(mn, mx);
+        double best = (double)cost.intersection * n;
+        int bax = -1;
+        float bp = 0.0f;
+        bool planar_left = false;
+        std::vector<Event> ev;
+        ev.reserve(2 * (size_t)n);
+        for (int a = 0; a < 3; a++) {
+            if (!(mx[a] > mn[a]) || !(sa > 0.0)) continue;
+            ev.clear();
+            for (int32_t t : list) {
+                const float l = std::max(lo[a][t], mn[a]), h = std::min(hi[a][t], mx[a]);
+                if (l == h) {
+                    ev.push_back({l, 1});
+                } else {
+                    ev.push_back({l, 2});
+                    ev.push_back({h, 0});
+                }
+            }
+            std::sort(ev.begin(), ev.end(), [](const Event &x, const Event &y) {
+                return x.p < y.p || (x.p == y.p && x.kind < y.kind);
+            });
+            // nl: triangles starting below p (or in an earlier plane);
+            // nr: triangles ending above p
+            int nl = 0, nr = n;
+            for (size_t i = 0; i < ev.size();) {
+                const float p = ev[i].p;
+                int ends = 0, planar = 0, starts = 0;
+                for (; i < ev.size() && ev[i].p == p && ev[i].kind == 0; i++) ends++;
+                for (; i < ev.size() && ev[i].p == p && ev[i].kind == 1; i++) planar++;
+                for (; i < ev.size() && ev[i].p == p && ev[i].kind == 2; i++) starts++;
+                nr -= planar + ends;
+                if (p > mn[a] && p < mx[a]) {
+                    float lmx[3] = {mx[0], mx[1], mx[2]}, rmn[3] = {mn[0], mn[1], mn[2]};
+                    lmx[a] = p;
+                    rmn[a] = p;
+                    const double pl = area(mn, lmx) / sa, pr = area(rmn, mx) / sa;
+                    for (int side = 0; side < 2; side++) {
+                        const int cl = nl + (side == 0 ? planar : 0);
+                        const int cr = nr + (side == 1 ? planar : 0);
+                        double c = cost.traversal + cost.intersection * (pl * cl + pr * cr);
+                        if (cl == 0 || cr == 0) c *= cost.empty_bonus;
+                        if (c < best) {
+                            best = c;
+                            bax = a;
+                            bp = p;
+                            planar_left = side == 0;
+                        }
+                    }
+                }
+                nl += starts + planar;
+            }
+        }
+        if (bax < 0) {
+            leaf(node, list);
+            return;
+        }
+        std::vector<int32_t> L, R;
+        for (int32_t t : list) {
+            const float l = std::max(lo[bax][t], mn[bax]), h = std::min(hi[bax][t], mx[bax]);
+            if (l == h && l == bp) {
+                (planar_left ? L : R).push_back(t);
+                continue;
+            }
+            if (l < bp) L.push_back(t);
+            if (h > bp) R.push_back(t);
+        }
+        std::vector<int32_t>().swap(list);
+        float lmx[3] = {mx[0], mx[1], mx[2]}, rmn[3] = {mn[0], mn[1], mn[2]};
+        lmx[bax] = bp;
+        rmn[bax] = bp;
+        const int left = (int)tree.children.size();
+        tree.children[node] = (uint32_t)bax + ((uint32_t)left << 2);
+        tree.split[node] = bp;
+        tree.children.push_back(0);
+        tree.children.push_back(0);
+        tree.split.push_back(0.0f);
+        tree.split.push_back(0.0f);
+        refine(left, std::move(L), mn, lmx, level + 1);
+        refine(left + 1, std::move(R), rmn, mx, level + 1);
+    }
+};
+
 }  // namespace
+
+void build_walk_tree(const std::vector<float> &xyz, const float *mn, const float *mx,
+                     const WalkTreeCosts &cost, HostTree &tree) {
+    const int64_t n = (int64_t)(xyz.size() / 9);
+    tree.children.assign(1, 0);
+    tree.split.assign(1, 0.0f);
+    tree.refs.clear();
+    tree.height = 0;
+    WalkBuilder b(xyz.data(), n, tree, cost);
+    std::vector<int32_t> root(n);
+    for (int64_t i = 0; i < n; i++) root[i] = (int32_t)i;
+    b.refine(0, std::move(root), mn, mx, 0);
+}
 
 void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, float *mx) {
     const int64_t n = (int64_t)(xyz.size() / 9);

@@ -206,6 +206,24 @@ class Environment:
         self._chk(self.lib.vrg_env_get_tree(self.h, _p(ch), _p(sp), _p(refs)), "get_tree")
         return ch, sp, refs[: nr.value], ht.value
 
+    def set_walk_tree_costs(self, traversal=1.0, intersection=1.5, empty_bonus=0.8,
+                            max_depth=28):
+        self._chk(self.lib.vrg_env_set_walk_tree_costs(self.h, traversal, intersection,
+                                                       empty_bonus, max_depth),
+                  "set_walk_tree_costs")
+
+    def walk_tree(self):
+        """The tree the device walks: (children, split, refs, height)."""
+        nn, nr, ht = C.c_int64(), C.c_int64(), C.c_int32()
+        self._chk(self.lib.vrg_env_walk_tree_info(self.h, C.byref(nn), C.byref(nr),
+                                                  C.byref(ht)), "walk_tree_info")
+        ch = np.zeros(nn.value, np.uint32)
+        sp = np.zeros(nn.value, np.float32)
+        refs = np.zeros(max(nr.value, 1), np.int32)
+        self._chk(self.lib.vrg_env_get_walk_tree(self.h, _p(ch), _p(sp), _p(refs)),
+                  "get_walk_tree")
+        return ch, sp, refs[: nr.value], ht.value
+
     def GetTriangle(self, index) -> bytes:
         buf = (C.c_uint8 * 48)()
         self._chk(self.lib.vrg_env_get_triangle(self.h, index, buf), "GetTriangle")
