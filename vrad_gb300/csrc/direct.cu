@@ -179,7 +179,8 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     const int nl = (int)env->lights.size();
     // variants: samples claimed per warp (32, 64, 128), 32 with the leaf
     // records kept out of L1, 32 in 4 x 2 luxel tiles without and with the
-    // top of the tree in shared memory; picked per bucket
+    // top of the tree in shared memory, and in tiles skipping children
+    // without triangles; picked per bucket
     auto launch = [&](int v) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
         if (e == cudaSuccess && d_rays) e = cudaMemsetAsync(d_rays, 0, 8, ctx->stream);
@@ -196,13 +197,15 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
             k_direct_luxels<32, kOptStream><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else if (v == 4)
             k_direct_luxels<32, 0, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else
+        else if (v == 5)
             k_direct_luxels<32, kOptTop, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+        else
+            k_direct_luxels<32, kOptSkip, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 6, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 7, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

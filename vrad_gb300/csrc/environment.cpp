@@ -112,17 +112,25 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     // triangle
     const HostTree &wt = env->walk_tree;
     const size_t nn = wt.children.size(), nr = wt.refs.size();
+    if (nn >= (size_t)kTopRef || nr >= ((size_t)1 << 30))
+        return fail(ctx, VRG_ERR_UNSUPPORTED, "kd tree too large for the device node format");
     std::vector<uint2> nodes(nn);
     for (size_t i = 0; i < nn; i++) {
-        uint32_t sbits;
+        uint32_t sbits, ch = wt.children[i];
         memcpy(&sbits, &wt.split[i], 4);
-        nodes[i] = make_uint2(wt.children[i], sbits);
+        if ((ch & 3u) != kLeaf) {  // flag children that are leaves without triangles
+            const uint32_t left = ch >> 2;
+            for (uint32_t c = 0; c < 2; c++)
+                if ((wt.children[left + c] & 3u) == kLeaf && wt.split[left + c] == 0.0f)
+                    ch |= c == 0 ? kLeftEmpty : kRightEmpty;
+        }
+        nodes[i] = make_uint2(ch, sbits);
     }
     // top table: breadth-first from the root, a pair of children at a
     // time, while it fits; children words of nodes whose children made it
     // into the table point into the table (index | kTopRef)
     std::vector<uint2> top;
-    if (nn < (size_t)kTopRef) {
+    {
         std::vector<int64_t> at(nn, -1);
         std::vector<uint32_t> order;  // node array index of each table entry
         top.push_back(nodes[0]);
@@ -131,7 +139,7 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         for (size_t q = 0; q < order.size(); q++) {
             const uint32_t x = order[q];
             if ((nodes[x].x & 3u) == kLeaf || top.size() + 2 > (size_t)kTopNodes) continue;
-            const uint32_t left = nodes[x].x >> 2;
+            const uint32_t left = (nodes[x].x >> 2) & kChildIndexMask;
             for (uint32_t c = 0; c < 2; c++) {
                 at[left + c] = (int64_t)top.size();
                 top.push_back(nodes[left + c]);
@@ -141,8 +149,10 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         for (size_t t = 0; t < top.size(); t++) {
             const uint32_t x = order[t];
             if ((nodes[x].x & 3u) == kLeaf) continue;
-            const int64_t l = at[nodes[x].x >> 2];
-            if (l >= 0) top[t].x = (nodes[x].x & 3u) | (((uint32_t)l | kTopRef) << 2);
+            const int64_t l = at[(nodes[x].x >> 2) & kChildIndexMask];
+            if (l >= 0)
+                top[t].x = (nodes[x].x & (3u | kLeftEmpty | kRightEmpty)) |
+                           (((uint32_t)l | kTopRef) << 2);
         }
     }
     env->ntop = (uint32_t)top.size();

@@ -227,8 +227,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
                     done = true;
             }
         } else if (run_node) {
-            node = inner_step(rp, nd, t0, t1, stk, sp);
-            nd = fetch_node<OPT>(s, node);
+            if (inner_step<OPT>(rp, nd, t0, t1, stk, sp, node) ||
+                pop_next<MODE>(stk, sp, best_t, node, t0, t1))
+                nd = fetch_node<OPT>(s, node);
+            else
+                done = true;
         }
         if (done) {
             active = false;
@@ -338,7 +341,7 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
 // lanes, with or without the vote, at the default or a 40-register cap,
 // leaf records kept out of L1 or not, top of the tree in shared memory or
-// not, next plane loaded ahead).
+// not, next plane loaded ahead, children without triangles skipped or not).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
@@ -347,6 +350,8 @@ const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1, kOptStream>,
     k_trace_unit<false, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<false, 8, false, 1, kOptStream | kOptTop>,
     k_trace_unit<false, 4, false, 1, kOptStream | kOptPipe>,
+    k_trace_mask<false, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptSkip>,
+    k_trace_unit<false, 8, true, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptStream | kOptSkip>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -356,8 +361,10 @@ const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1, kOptStream>,
     k_trace_unit<true, 4, false, 1, kOptStream | kOptTop>, k_trace_unit<true, 8, false, 1, kOptStream | kOptTop>,
     k_trace_unit<true, 4, false, 1, kOptStream | kOptPipe>,
+    k_trace_mask<true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptSkip>,
+    k_trace_unit<true, 8, true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptStream | kOptSkip>,
 };
-constexpr int kMaskVariants = 12;
+constexpr int kMaskVariants = 16;
 
 }  // namespace
 

@@ -55,7 +55,15 @@ struct DevScene {
 // has kTopRef set points into the table instead of the node array, so a
 // walk that stages the table in shared memory reads the top levels there.
 constexpr int kTopNodes = 512;
-constexpr uint32_t kTopRef = 1u << 28;
+constexpr uint32_t kTopRef = 1u << 27;
+
+// Children word of an inner node on the device: axis (bits 0-1), index of
+// the left child with kTopRef (bits 2-29), and whether the left (bit 31) or
+// the right (bit 30) child is a leaf without triangles, so that the walk
+// never fetches or stacks such a child.  Leaf words are 3 | first record << 2.
+constexpr uint32_t kLeftEmpty = 1u << 31;
+constexpr uint32_t kRightEmpty = 1u << 30;
+constexpr uint32_t kChildIndexMask = (1u << 28) - 1u;  // after >> 2
 
 // Lightmapped face, 80 bytes.
 struct alignas(16) FaceRec {

@@ -33,6 +33,7 @@ constexpr int32_t kTraceIdSky = 0x01000000;
 constexpr int kOptStream = 1;
 constexpr int kOptTop = 2;
 constexpr int kOptPipe = 8;    // unit rounds: the next triangle's plane loads during this test
+constexpr int kOptSkip = 16;   // children flagged as leaves without triangles are not visited
 
 // Shared-memory copy of the scene's top table, for kernels walking with
 // kOptTop (allocated only in kernels that use it).
@@ -160,33 +161,41 @@ __device__ __forceinline__ bool trace_init(const DevScene &s, const Ray &ray, co
     return st.t0 <= st.t1;
 }
 
-// One step through an inner node: returns the child that holds the first
-// part of [t0, t1] and narrows the interval to it; the other child is pushed
-// (with its part of the interval) when the ray reaches it too.  The stack
-// never overflows: it holds at most one entry per tree level.
-__device__ __forceinline__ uint32_t inner_step(const RayPre &rp, uint2 nd, float &t0, float &t1,
-                                               uint4 *stk, int &sp) {
+// One step through an inner node: sets `next` to the child that holds the
+// first part of [t0, t1] and narrows the interval to it; the other child is
+// pushed (with its part of the interval) when the ray reaches it too.  With
+// kOptSkip children without triangles are neither entered nor pushed, and
+// the step returns false when no child is left to visit (without it, it
+// always returns true).  The stack never overflows: it holds at most one
+// entry per tree level.
+template <int OPT>
+__device__ __forceinline__ bool inner_step(const RayPre &rp, uint2 nd, float &t0, float &t1,
+                                           uint4 *stk, int &sp, uint32_t &next) {
     const uint32_t type = nd.x & 3u;
     const float sv = __uint_as_float(nd.y);
-    const uint32_t left = nd.x >> 2;
+    const uint32_t left = (nd.x >> 2) & kChildIndexMask;
     const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
     const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
     const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
     const uint32_t neg = (rp.neg >> type) & 1u;
     const uint32_t nearc = left + neg, farc = left + 1u - neg;
+    const bool near_empty = (OPT & kOptSkip) && (nd.x & (neg ? kRightEmpty : kLeftEmpty)) != 0u;
+    const bool far_empty = (OPT & kOptSkip) && (nd.x & (neg ? kLeftEmpty : kRightEmpty)) != 0u;
     const float tne = __fmaf_rn(sv, inv, A);
     const float tfe = __fmaf_rn(sv, inv, B);
-    const bool vn = !(tne < t0), vf = !(tfe > t1);
+    const bool vn = !(tne < t0) && !near_empty, vf = !(tfe > t1) && !far_empty;
     if (vn) {
         if (vf && sp < kStackMax) {
             stk[sp] = make_uint4(farc, __float_as_uint(fmaxf(t0, tfe)), __float_as_uint(t1), 0u);
             sp++;
         }
         t1 = fminf(t1, tne);
-        return nearc;
+        next = nearc;
+        return true;
     }
     t0 = fmaxf(t0, tfe);
-    return farc;
+    next = farc;
+    return (OPT & kOptSkip) ? vf : true;
 }
 
 // Ray/triangle test (project semantics, in this operation order):
@@ -305,12 +314,16 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
     float t0 = st.t0, t1 = st.t1;
     int sp = st.sp;
     uint2 nd = fetch_node<OPT>(s, node);
+    bool reached = true;
     while ((nd.x & 3u) != 3u) {
-        node = inner_step(rp, nd, t0, t1, st.stk, sp);
+        if (!inner_step<OPT>(rp, nd, t0, t1, st.stk, sp, node)) {
+            reached = false;
+            break;
+        }
         nd = fetch_node<OPT>(s, node);
     }
-    if (leaf_test<MODE, LB, OPT>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
-                            (int)__uint_as_float(nd.y), st.best, st.best_t))
+    if (reached && leaf_test<MODE, LB, OPT>(s, ray, tmin, tmax, skip, any_limit, nd.x >> 2,
+                                            (int)__uint_as_float(nd.y), st.best, st.best_t))
         return true;
     if (!pop_next<MODE>(st.stk, sp, st.best_t, st.node, st.t0, st.t1))
         return true;
