@@ -108,15 +108,16 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def _cpu_baseline(lit, faces, threads, walk_tree=None):
+def _cpu_baseline(lit, faces, threads, walk_tree=None, skip_empty=False):
     """Oracle gather over faces [0, faces): shadow rays, seconds, walk stats.
-    walk_tree: walk that tree instead of the reference's (for counting the
-    device's node and triangle reads)."""
+    walk_tree / skip_empty: walk that tree, as the device does, instead of
+    the reference's (for counting the device's node and triangle reads)."""
     from oracle import pyoracle
 
     s = pyoracle.Scene(lit.xyz, lit.ids)
     if walk_tree is not None:
         s.set_tree(*walk_tree)
+        s.set_skip_empty(skip_empty)
     lights = pyoracle.make_lights(lit.lights)
     t0 = time.perf_counter()
     _, rays, st = pyoracle.gather_luxels(s, lights, len(lit.lights), lit, 0, faces, ss=4,
@@ -335,6 +336,11 @@ def run_gpu(args, rank, world, local_rank):
     cpu = None
     roof = None
     avg_ms = kms / max(kn, 1)
+    tkey = (Context.tune_key("trace_mask", env.num_triangles(), n) if args.workload == "anyhit"
+            else Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
+    tv, tms = lib_ctx.autotune_choice(tkey)
+    # variants that never visit leaves without triangles (kOptSkip)
+    skip_empty = tv in ((12, 13, 14, 15) if args.workload == "anyhit" else (6,))
     if args.workload == "anyhit":
         from oracle import pyoracle
 
@@ -344,6 +350,7 @@ def run_gpu(args, rank, world, local_rank):
         dt = time.perf_counter() - t0
         # node and triangle counts of the walk the device does (its own tree)
         s.set_tree(*env.walk_tree()[:3])
+        s.set_skip_empty(skip_empty)
         _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
         nodes, tris = st[:, 0].mean(), st[:, 1].mean()
         # per line: end points, mask bit, and per node / per triangle test the
@@ -355,7 +362,7 @@ def run_gpu(args, rank, world, local_rank):
         cpu_faces = min(CPU_SAMPLE_FACES, lit.n_faces)
         rays_cpu, dt, _ = _cpu_baseline(lit, cpu_faces, threads, None)
         _, _, st = _cpu_baseline(lit, min(STATS_SAMPLE_FACES, lit.n_faces), threads,
-                                 env.walk_tree()[:3])
+                                 env.walk_tree()[:3], skip_empty)
         nodes, tris = st[1] / st[0], st[2] / st[0]
         # per shadow line: nodes and leaf records as above, plus the sample's
         # position and normal (24 B) and its share of the RGB output (12 B per
@@ -366,12 +373,9 @@ def run_gpu(args, rank, world, local_rank):
                "kind": "port",
                "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
     achieved = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
-    tkey = (Context.tune_key("trace_mask", env.num_triangles(), n) if args.workload == "anyhit"
-            else Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
-    tv, tms = lib_ctx.autotune_choice(tkey)
     # DRAM traffic per launch from the committed ncu capture of the variant family in use
     prof = f"ncu_{kernel}.txt"
-    if args.workload == "anyhit" and tv in (6, 7, 9, 10, 11):  # unit rounds, leaf records out of L1
+    if args.workload == "anyhit" and tv in (6, 7, 9, 10, 11, 15):  # unit rounds, leaf records out of L1
         prof = "ncu_trace_unit_stream.txt"
     traffic = _ncu_traffic(prof)
     torch.cuda.synchronize()

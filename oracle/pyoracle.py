@@ -118,6 +118,10 @@ class Scene:
         if rc != 0:
             raise RuntimeError("orc_scene_set_tree failed")
 
+    def set_skip_empty(self, on: bool):
+        """Walk as the library's kOptSkip variants do (for node counts)."""
+        lib().orc_scene_set_skip_empty(C.c_void_p(self.h), int(bool(on)))
+
     def tris(self):
         out = (OTri * max(self.n, 1))()
         lib().orc_scene_get_tris(C.c_void_p(self.h), out)

@@ -52,6 +52,7 @@ struct orc_scene {
     float sky_min[3], sky_max[3];
     int mode;
     int depth;
+    int skip_empty; /* walk: do not visit leaves without triangles (same answers) */
 };
 
 /* ------------------------------------------------------------------ */
@@ -407,6 +408,8 @@ int orc_scene_set_tree(orc_scene *s, const uint32_t *children, const float *spli
     return 0;
 }
 
+void orc_scene_set_skip_empty(orc_scene *s, int on) { s->skip_empty = on != 0; }
+
 void orc_scene_get_tris(const orc_scene *s, orc_tri *out) {
     memcpy(out, s->tris, sizeof(orc_tri) * (size_t)s->ntris);
 }
@@ -460,6 +463,10 @@ static float ray_slack(const orc_scene *s, const float *o) {
     return 7.62939453125e-06f * ((s->coord_scale + om) + 1.0f);
 }
 
+static int empty_leaf(const orc_scene *s, uint32_t node) {
+    return (int)(s->children[node] & 3u) == KD_LEAF && s->split[node] == 0.0f;
+}
+
 /* Walks the tree; closest = 0 stops at the first accepted hit.  Results are
  * identical to testing every triangle (brute force): for closest hits the
  * minimum t wins and equal t goes to the lower triangle index. */
@@ -497,6 +504,10 @@ static int trace_kd(const orc_scene *s, const float *o, const float *d, float tm
             float tne = ((sv + sd) - o[type]) * inv[type];
             float tfe = ((sv - sd) - o[type]) * inv[type];
             int vn = !(tne < t0), vf = !(tfe > t1);
+            if (s->skip_empty) { /* the library's kOptSkip walk: never enter an empty leaf */
+                vn = vn && !empty_leaf(s, near);
+                vf = vf && !empty_leaf(s, far);
+            }
             if (vn && vf) {
                 stack[sp].node = far;
                 stack[sp].t0 = fmaxf(t0, tfe);

@@ -83,6 +83,9 @@ int64_t orc_scene_num_nodes(const orc_scene *s);
 int64_t orc_scene_num_refs(const orc_scene *s);
 void orc_scene_get_tree(const orc_scene *s, uint32_t *children, float *split, int32_t *refs);
 void orc_scene_get_tris(const orc_scene *s, orc_tri *out);
+/* walk without visiting leaves that hold no triangle (answers unchanged;
+ * only the node counts of the stats differ) */
+void orc_scene_set_skip_empty(orc_scene *s, int on);
 /* replace the tree (same format as orc_scene_get_tree); 0 on success */
 int orc_scene_set_tree(orc_scene *s, const uint32_t *children, const float *split,
                        int64_t nnodes, const int32_t *refs, int64_t nrefs);

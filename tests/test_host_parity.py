@@ -93,6 +93,15 @@ def test_walk_tree_gives_the_reference_trees_answers(oracle, host_ctx, which, an
     hw, tw = walk.trace_closest(o, d[:4000], 0.0, 1.0, threads=16)
     assert np.array_equal(hb, hw) and bits_equal(tb, tw)
     assert np.array_equal(walk.test_lines(a, b, threads=16), ref.test_lines(a, b, threads=16))
+    # the walk that never enters leaves without triangles: same answers and
+    # fewer nodes on average (a far child it descends into directly skips
+    # the closest-hit pruning a pop applies, so a few lines visit more)
+    _, _, _, st0 = walk.occlusion_mask(a, b, threads=16, closest=True, stats=True)
+    walk.set_skip_empty(True)
+    m2, h2, t2, st2 = walk.occlusion_mask(a, b, threads=16, closest=True, stats=True)
+    assert np.array_equal(m0, m2) and np.array_equal(h0, h2) and bits_equal(t0, t2)
+    assert st2[:, 0].mean() < st0[:, 0].mean()
+    assert np.mean(st2[:, 0] > st0[:, 0]) < 0.01
 
 
 @pytest.mark.parametrize("n", [0, 1, 2, 3, 7, 25])
