@@ -375,7 +375,9 @@ def run_gpu(args, rank, world, local_rank):
     achieved = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
     # DRAM traffic per launch from the committed ncu capture of the variant family in use
     prof = f"ncu_{kernel}.txt"
-    if args.workload == "anyhit" and tv in (6, 7, 9, 10, 11, 15):  # unit rounds, leaf records out of L1
+    if args.workload == "anyhit" and tv in (13, 14, 15):  # unit rounds skipping empty children
+        prof = "ncu_trace_unit_skip.txt"
+    elif args.workload == "anyhit" and tv in (6, 7, 9, 10, 11):  # unit rounds, leaf records out of L1
         prof = "ncu_trace_unit_stream.txt"
     traffic = _ncu_traffic(prof)
     torch.cuda.synchronize()
