@@ -98,7 +98,7 @@ def test_transfer_variants_identical(gpu_ctx, tmp_path):
     dirs = scenes.transfer_directions(k)
     key = Context.tune_key("transfer_rows", env.num_triangles(), nl * k)
     ref = None
-    for v in range(4):
+    for v in range(6):
         _force(gpu_ctx, tmp_path, key, v)
         nnz = env.make_transfers(dirs)
         got = env.get_transfers(nl, nnz)

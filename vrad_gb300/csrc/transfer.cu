@@ -212,14 +212,18 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k) {
     VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // `dirs` is pageable and goes out of scope
     const size_t smem = 2 * (size_t)k * sizeof(int32_t);
     // variants, picked per (triangles, rows) bucket: 256 or 512 threads per
-    // row block, leaf records through L1 or not
+    // row block, leaf records through L1 or not, children without triangles
+    // visited or skipped
     using RowKernel = void (*)(DevScene, const LeafInfo *, const FaceRec *, const PatchNode *, const int32_t *,
                                const int32_t *, const float *, int, int64_t, int64_t, int32_t *, int32_t *,
                                int32_t *);
-    const RowKernel kvar[4] = {k_transfer_rows<256, 0>, k_transfer_rows<512, 0>,
-                               k_transfer_rows<256, kOptStream>, k_transfer_rows<512, kOptStream>};
-    const int vthreads[4] = {256, 512, 256, 512};
-    for (int v = 0; v < 4; v++)
+    constexpr int kRowVariants = 6;
+    const RowKernel kvar[kRowVariants] = {k_transfer_rows<256, 0>,          k_transfer_rows<512, 0>,
+                                          k_transfer_rows<256, kOptStream>, k_transfer_rows<512, kOptStream>,
+                                          k_transfer_rows<256, kOptSkip>,   k_transfer_rows<512, kOptSkip>};
+    const int vthreads[kRowVariants] = {256, 512, 256, 512, 256, 512};
+    const int twin256[kRowVariants] = {0, 0, 2, 2, 4, 4};  // the 256-thread variant with the same options
+    for (int v = 0; v < kRowVariants; v++)
         VRG_CUDA(ctx, cudaFuncSetAttribute(kvar[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // rows go through in chunks whose staging stays near 1 GiB
     const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(rows, ((int64_t)1 << 30) / (8 * (int64_t)k)));
@@ -240,7 +244,7 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k) {
             const int threads = std::min(vthreads[v], k);
             // a row block never has more threads than rays: below 512 rays the
             // 512-thread variants fall back to their 256-thread twin
-            const int vv = threads == vthreads[v] ? v : (v & 2);
+            const int vv = threads == vthreads[v] ? v : twin256[v];
             kvar[vv]<<<grid, threads, smem, ctx->stream>>>(
                 s, env->d_leaf_info.as<LeafInfo>(), env->d_faces.as<FaceRec>(),
                 env->d_patch_nodes.as<PatchNode>(), env->d_face_root.as<int32_t>(), env->d_tri_face.as<int32_t>(),
@@ -250,7 +254,8 @@ int run_make_transfers(vrg_env *env, const float *dirs_local, int32_t k) {
             timing_end(ctx, "transfer_rows", ev);
             return e;
         };
-        const int rc = tune_run(ctx, tune_key("transfer_rows", env->geom.ntris, rows * (int64_t)k), 4, launch);
+        const int rc = tune_run(ctx, tune_key("transfer_rows", env->geom.ntris, rows * (int64_t)k), kRowVariants,
+                                launch);
         if (rc != VRG_OK) return rc;
         VRG_CUDA(ctx, cudaMemcpyAsync(h_nnz.data(), d_nnz.ptr, 4 * (size_t)nr, cudaMemcpyDeviceToHost, ctx->stream));
         VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
