@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(NT) k_transfer_rows(
         const float qx = radd(li.center.x, rmul(F.normal.x, kSampleOffset));
         const float qy = radd(li.center.y, rmul(F.normal.y, kSampleOffset));
         const float qz = radd(li.center.z, rmul(F.normal.z, kSampleOffset));
-        const float il = rdiv(1.0f, rsqrt_rn(dot3r(F.u.x, F.u.y, F.u.z, F.u.x, F.u.y, F.u.z)));
+        const float il = rrcp(rsqrt_rn(dot3r(F.u.x, F.u.y, F.u.z, F.u.x, F.u.y, F.u.z)));
         const float t1x = rmul(F.u.x, il), t1y = rmul(F.u.y, il), t1z = rmul(F.u.z, il);
         const float nx = F.normal.x, ny = F.normal.y, nz = F.normal.z;
         const float t2x = rsub(rmul(ny, t1z), rmul(nz, t1y));

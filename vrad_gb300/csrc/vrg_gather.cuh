@@ -71,7 +71,7 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
             if (radius > 0.0f && dist2 > rmul(radius, radius)) continue;
             if (dist2 == 0.0f) continue;
             const float dist = rsqrt_rn(dist2);
-            const float inv = rdiv(1.0f, dist);
+            const float inv = rrcp(dist);
             const float Lx = rmul(dlx, inv), Ly = rmul(dly, inv), Lz = rmul(dlz, inv);
             const float cosr = dot3r(nx, ny, nz, Lx, Ly, Lz);
             if (!(cosr > 0.0f)) continue;
@@ -83,7 +83,7 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
             }
             const float denom = radd(radd(at.x, rmul(at.y, dc)), rmul(at.z, dc2));
             if (!(denom > 0.0f)) continue;
-            float f = rdiv(1.0f, denom);
+            float f = rrcp(denom);
             const float4 cn = __ldg(&lights[li].cone);
             if (cn.w > cn.z && dist > cn.z) {
                 if (dist >= cn.w) continue;
@@ -167,7 +167,7 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
 __device__ __forceinline__ void luxel_sample(const FaceRec &f, int64_t lux, int iu, int iv, int k,
                                              int ss, uint64_t seed, float &px, float &py,
                                              float &pz) {
-    const float inu = rdiv(1.0f, (float)f.nu), inv = rdiv(1.0f, (float)f.nv);
+    const float inu = rrcp((float)f.nu), inv = rrcp((float)f.nv);
     float su, sv;
     if (ss == 4) {
         const uint64_t h = splitmix(seed, (uint64_t)(lux * 4 + k));

@@ -17,6 +17,9 @@ __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+// 1 / b rounded to nearest: the same float as rdiv(1.0f, b) (both are the
+// correctly rounded quotient), with a shorter instruction sequence
+__device__ __forceinline__ float rrcp(float b) { return __frcp_rn(b); }
 __device__ __forceinline__ float rsqrt_rn(float a) { return __fsqrt_rn(a); }
 __device__ __forceinline__ float dot3r(float ax, float ay, float az, float bx, float by, float bz) {
     return radd(radd(rmul(ax, bx), rmul(ay, by)), rmul(az, bz));
@@ -365,7 +368,7 @@ __device__ __forceinline__ Line make_line(float sx, float sy, float sz, float ex
     L.oz = sz;
     float dx = rsub(ex, sx), dy = rsub(ey, sy), dz = rsub(ez, sz);
     L.len = rsqrt_rn(dot3r(dx, dy, dz, dx, dy, dz));
-    const float r = rdiv(1.0f, L.len);
+    const float r = rrcp(L.len);
     L.dx = rmul(dx, r);
     L.dy = rmul(dy, r);
     L.dz = rmul(dz, r);
