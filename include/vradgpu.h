@@ -139,12 +139,13 @@ int vrg_env_add_axis_aligned_rectangular_solid(vrg_env *env, int32_t id, const f
 /* Bulk AddTriangle for n triangles (xyz: 9 floats each), the loop of
  * cmd/tasks/loadbsp/main.go:276,338. */
 int vrg_env_add_triangles(vrg_env *env, const float *xyz, const int32_t *ids, int64_t n);
-/* SetupAccelerationStructure (environment.go:119-138): SAH kd tree built on
- * the host with the reference's candidates, costs and partition order.  The
- * device walks a second tree of the same format built with every candidate
- * plane (the walk tree); it is uploaded with the intersection records and
- * stays resident.  Both trees give the same answers: every query returns
- * what testing every triangle would. */
+/* SetupAccelerationStructure (environment.go:119-138): builds on the host
+ * and uploads the tree the device walks (the walk tree: the reference's node
+ * format, SAH over every candidate plane) with the intersection records;
+ * they stay resident.  The reference's own tree (its candidates, costs and
+ * partition order) is built when vrg_env_tree_info or vrg_env_get_tree first
+ * asks for it.  Both trees give the same answers: every query returns what
+ * testing every triangle would. */
 int vrg_env_setup_acceleration_structure(vrg_env *env);
 int64_t vrg_env_num_triangles(const vrg_env *env);
 /* Size of the reference's tree: nodes, triangle-index-list length, height. */

@@ -76,7 +76,11 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     vrg_ctx *ctx = env->ctx;
     const int64_t n = (int64_t)env->ids.size();
     if (n >= (int64_t)1 << 30) return fail(ctx, VRG_ERR_UNSUPPORTED, "more than 2^30 triangles");
-    build_kd_tree(env->xyz, env->tree, env->min_bound, env->max_bound);
+    // the reference's tree is built when first asked for (vrg_env_tree_info /
+    // vrg_env_get_tree): the device walks the walk tree
+    scene_bounds(env->xyz, env->min_bound, env->max_bound);
+    env->tree = HostTree();
+    env->ref_tree_built = false;
     build_walk_tree(env->xyz, env->min_bound, env->max_bound, env->walk_costs, env->walk_tree);
     if (env->walk_tree.height >= kStackMax)
         return fail(ctx, VRG_ERR_UNSUPPORTED, "kd tree deeper than the traversal stack");
@@ -190,8 +194,23 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     return VRG_OK;
 }
 
+namespace {
+// Builds the reference's tree on first use (under the environment's lock).
+const HostTree &reference_tree(const vrg_env *cenv) {
+    vrg_env *env = const_cast<vrg_env *>(cenv);
+    std::lock_guard<std::mutex> lk(env->mu);
+    if (!env->ref_tree_built) {
+        float mn[3], mx[3];
+        build_kd_tree(env->xyz, env->tree, mn, mx);
+        env->ref_tree_built = true;
+    }
+    return env->tree;
+}
+}  // namespace
+
 int vrg_env_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height) {
     if (!env || !env->built) return VRG_ERR_STATE;
+    reference_tree(env);
     if (nodes) *nodes = (int64_t)env->tree.children.size();
     if (refs) *refs = (int64_t)env->tree.refs.size();
     if (height) *height = env->tree.height;
@@ -200,6 +219,7 @@ int vrg_env_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t
 
 int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs) {
     if (!env || !env->built) return VRG_ERR_STATE;
+    reference_tree(env);
     if (children) memcpy(children, env->tree.children.data(), env->tree.children.size() * 4);
     if (split) memcpy(split, env->tree.split.data(), env->tree.split.size() * 4);
     if (refs) memcpy(refs, env->tree.refs.data(), env->tree.refs.size() * 4);

@@ -308,12 +308,8 @@ void build_walk_tree(const std::vector<float> &xyz, const float *mn, const float
     b.refine(0, std::move(root), mn, mx, 0);
 }
 
-void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, float *mx) {
+void scene_bounds(const std::vector<float> &xyz, float *mn, float *mx) {
     const int64_t n = (int64_t)(xyz.size() / 9);
-    tree.children.assign(1, 0);
-    tree.split.assign(1, 0.0f);
-    tree.refs.clear();
-    tree.height = 0;
     for (int a = 0; a < 3; a++) {
         mn[a] = 1.0e23f;
         mx[a] = -1.0e23f;
@@ -324,6 +320,15 @@ void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, flo
     }
     if (n == 0)
         for (int a = 0; a < 3; a++) mn[a] = mx[a] = 0.0f;
+}
+
+void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, float *mx) {
+    const int64_t n = (int64_t)(xyz.size() / 9);
+    tree.children.assign(1, 0);
+    tree.split.assign(1, 0.0f);
+    tree.refs.clear();
+    tree.height = 0;
+    scene_bounds(xyz, mn, mx);
     Builder b(xyz.data(), n, tree);
     std::vector<int32_t> root(n);
     for (int64_t i = 0; i < n; i++) root[i] = (int32_t)i;

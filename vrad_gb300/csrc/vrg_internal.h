@@ -126,7 +126,8 @@ struct vrg_env {
     float min_bound[3] = {0, 0, 0}, max_bound[3] = {0, 0, 0};
 
     bool built = false;
-    HostTree tree;        // the reference's tree (SetupAccelerationStructure)
+    HostTree tree;        // the reference's tree, built on first request
+    bool ref_tree_built = false;
     HostTree walk_tree;   // the tree the device walks (build_walk_tree)
     WalkTreeCosts walk_costs;
     std::vector<vrg::TriRecord> tri_records;  // per triangle, insertion order
@@ -217,6 +218,7 @@ void tri_intersect_format(const float *xyz9, int32_t id, uint8_t flags, TriRecor
                           uint32_t tri_index);
 void edge_equation(const float *p1, const float *p2, int c1, int c2, const float *inside,
                    float *out3);
+void scene_bounds(const std::vector<float> &xyz, float *mn, float *mx);
 void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, float *mx);
 void build_walk_tree(const std::vector<float> &xyz, const float *mn, const float *mx,
                      const WalkTreeCosts &cost, HostTree &tree);
