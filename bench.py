@@ -108,16 +108,19 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def _cpu_baseline(lit, faces, threads, walk_tree=None, skip_empty=False):
+def _cpu_baseline(lit, faces, threads, walk_tree=None, skip_empty=False, walls=None):
     """Oracle gather over faces [0, faces): shadow rays, seconds, walk stats.
-    walk_tree / skip_empty: walk that tree, as the device does, instead of
-    the reference's (for counting the device's node and triangle reads)."""
+    walk_tree / skip_empty / walls: walk as the device does (its tree, its
+    options, its wall test) instead of the reference's way, for counting
+    the device's node and triangle reads."""
     from oracle import pyoracle
 
     s = pyoracle.Scene(lit.xyz, lit.ids)
     if walk_tree is not None:
         s.set_tree(*walk_tree)
         s.set_skip_empty(skip_empty)
+    if walls is not None:
+        s.set_walls(*walls)
     lights = pyoracle.make_lights(lit.lights)
     t0 = time.perf_counter()
     _, rays, st = pyoracle.gather_luxels(s, lights, len(lit.lights), lit, 0, faces, ss=4,
@@ -362,7 +365,7 @@ def run_gpu(args, rank, world, local_rank):
         cpu_faces = min(CPU_SAMPLE_FACES, lit.n_faces)
         rays_cpu, dt, _ = _cpu_baseline(lit, cpu_faces, threads, None)
         _, _, st = _cpu_baseline(lit, min(STATS_SAMPLE_FACES, lit.n_faces), threads,
-                                 env.walk_tree()[:3], skip_empty)
+                                 env.walk_tree()[:3], skip_empty, env.wall_slots())
         nodes, tris = st[1] / st[0], st[2] / st[0]
         # per shadow line: nodes and leaf records as above, plus the sample's
         # position and normal (24 B) and its share of the RGB output (12 B per
@@ -387,8 +390,9 @@ def run_gpu(args, rank, world, local_rank):
             "peak_kind": f"{peak_kind} HBM copy",
             "kernel": kernel, "kernel_ms": round(avg_ms, 4),
             "bytes_per_ray": round(bytes_per_unit, 2),
-            "bytes_model": "8 per kd node + 48 per triangle test (leaf-ordered records), means "
-                           "of the oracle's walk of the device's tree over the same lines" +
+            "bytes_model": "8 per kd node + 48 per triangle test (leaf-ordered records and wall "
+                           "slots), means of the oracle's walk of the device's tree, with the "
+                           "device's options and wall test, over the same lines" +
                            (" + 24 end points + 1/8 mask"
                            if args.workload == "anyhit" else " + sample position, normal and RGB share"),
             "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),

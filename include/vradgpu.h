@@ -158,6 +158,12 @@ int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32
  * before vrg_env_setup_acceleration_structure. */
 int vrg_env_set_walk_tree_costs(vrg_env *env, float traversal, float intersection,
                                 float empty_bonus, int32_t max_depth);
+/* Wall slots: per face of the scene box (face 2*axis + 1 for a max side),
+ * up to 4 opaque triangles lying in that face, largest first (tris[4*face+i],
+ * -1 unused).  A shadow line of the direct-light gathers first tests the
+ * slots of the face it leaves the box through: a hit before the sky region
+ * occludes it whatever lies in between, so the walk is skipped. */
+int vrg_env_wall_slots(const vrg_env *env, int32_t *tris, int32_t *counts);
 /* The walk tree, in the format of vrg_env_tree_info / vrg_env_get_tree. */
 int vrg_env_walk_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height);
 int vrg_env_get_walk_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs);

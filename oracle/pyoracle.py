@@ -122,6 +122,16 @@ class Scene:
         """Walk as the library's kOptSkip variants do (for node counts)."""
         lib().orc_scene_set_skip_empty(C.c_void_p(self.h), int(bool(on)))
 
+    def set_walls(self, tris=None, counts=None):
+        """Test each shadow line's exit-face wall triangles first, as the
+        library does (tris: 6 x 4 triangle indices, counts: 6); None: off."""
+        if tris is None:
+            lib().orc_scene_set_walls(C.c_void_p(self.h), None, None)
+            return
+        t = np.ascontiguousarray(tris, np.int32).reshape(24)
+        c = np.ascontiguousarray(counts, np.int32).reshape(6)
+        lib().orc_scene_set_walls(C.c_void_p(self.h), _p(t), _p(c))
+
     def tris(self):
         out = (OTri * max(self.n, 1))()
         lib().orc_scene_get_tris(C.c_void_p(self.h), out)

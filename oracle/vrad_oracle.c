@@ -53,6 +53,9 @@ struct orc_scene {
     int mode;
     int depth;
     int skip_empty; /* walk: do not visit leaves without triangles (same answers) */
+    int use_walls;  /* shadow lines test the wall triangles of their exit face first */
+    int32_t walls[6][4];
+    int nwalls[6];
 };
 
 /* ------------------------------------------------------------------ */
@@ -410,6 +413,20 @@ int orc_scene_set_tree(orc_scene *s, const uint32_t *children, const float *spli
 
 void orc_scene_set_skip_empty(orc_scene *s, int on) { s->skip_empty = on != 0; }
 
+void orc_scene_set_walls(orc_scene *s, const int32_t *tris, const int32_t *counts) {
+    s->use_walls = 0;
+    for (int f = 0; f < 6; f++) {
+        s->nwalls[f] = 0;
+        if (!tris || !counts) continue;
+        for (int i = 0; i < counts[f] && i < 4; i++) {
+            const int32_t t = tris[4 * f + i];
+            if (t < 0 || t >= s->ntris) continue;
+            s->walls[f][s->nwalls[f]++] = t;
+            s->use_walls = 1;
+        }
+    }
+}
+
 void orc_scene_get_tris(const orc_scene *s, orc_tri *out) {
     memcpy(out, s->tris, sizeof(orc_tri) * (size_t)s->ntris);
 }
@@ -609,6 +626,49 @@ static int trace_one(const orc_scene *s, const float *o, const float *d, float t
  *   trace [0, len) skipping triangles whose id == skip_id
  *   occluded iff the closest hit has t < len and its id lacks TRACE_ID_SKY.
  * Returns 1 when occluded.  A zero-length line is never occluded. */
+/* The library's wall test (its shadow lines' shortcut, same verdicts): the
+ * face of the slack-padded scene box the line leaves through, and the
+ * opaque triangles set for it (orc_scene_set_walls) tested first.  A hit
+ * before any_limit -- the entry into the sky triangles' box padded by
+ * 2*slack, before which no sky triangle can be hit -- occludes the line
+ * whatever lies in front of it.  *tests counts the triangles tested. */
+static int wall_occludes(const orc_scene *s, const float *a, const float *dir, float len,
+                         int32_t skip, uint32_t *tests) {
+    const float slack = ray_slack(s, a);
+    int f = 0;
+    float tex = INFINITY;
+    for (int ax = 0; ax < 3; ax++) {
+        const int neg = signbit(dir[ax]) != 0;
+        const float bound = neg ? s->bmin[ax] - slack : s->bmax[ax] + slack;
+        const float t = (bound - a[ax]) / dir[ax];
+        if (t < tex) {
+            tex = t;
+            f = 2 * ax + (neg ? 0 : 1);
+        }
+    }
+    if (!(tex < 2.0f * len)) return 0;
+    float any_limit = INFINITY;
+    if (s->has_sky) {
+        float ts0 = -INFINITY, ts1 = INFINITY;
+        for (int ax = 0; ax < 3; ax++) {
+            const float ta = ((s->sky_min[ax] - 2.0f * slack) - a[ax]) / dir[ax];
+            const float tb = ((s->sky_max[ax] + 2.0f * slack) - a[ax]) / dir[ax];
+            const int neg = signbit(dir[ax]) != 0;
+            ts0 = fmaxf(ts0, neg ? tb : ta);
+            ts1 = fminf(ts1, neg ? ta : tb);
+        }
+        if (ts0 <= ts1 && ts0 < len) any_limit = ts0;
+    }
+    for (int i = 0; i < s->nwalls[f]; i++) {
+        const orc_tri *tr = &s->tris[s->walls[f][i]];
+        if (tr->id == skip) continue;
+        (*tests)++;
+        float th;
+        if (tri_hit(tr, a, dir, 0.0f, len, &th) && th < any_limit) return 1;
+    }
+    return 0;
+}
+
 static int line_occluded(const orc_scene *s, const float *a, const float *b, int32_t skip,
                          int brute, int32_t *hit_out, float *t_out, uint32_t *st) {
     float dir[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
@@ -625,7 +685,14 @@ static int line_occluded(const orc_scene *s, const float *a, const float *b, int
         if (t_out) *t_out = INFINITY;
         return 0;
     }
+    uint32_t wall_tests = 0;
+    if (s->use_walls && !hit_out && !t_out && !brute &&
+        wall_occludes(s, a, dir, len, skip, &wall_tests)) {
+        if (st) st[1] = wall_tests;
+        return 1;
+    }
     trace_one(s, a, dir, 0.0f, len, skip, 1, brute, &hit, &th, st);
+    if (st) st[1] += wall_tests;
     if (hit_out) *hit_out = hit;
     if (t_out) *t_out = th;
     return hit >= 0 && th < len && (s->tris[hit].id & ORC_TRACE_ID_SKY) == 0;

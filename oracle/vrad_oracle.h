@@ -86,6 +86,11 @@ void orc_scene_get_tris(const orc_scene *s, orc_tri *out);
 /* walk without visiting leaves that hold no triangle (answers unchanged;
  * only the node counts of the stats differ) */
 void orc_scene_set_skip_empty(orc_scene *s, int on);
+/* shadow lines (no hit output) first test the opaque triangles lying in
+ * the scene-box face they leave through, as the library does: tris[4*f+i]
+ * for i < counts[f] (face f = 2*axis + 1 for a max side); NULL: off.
+ * Verdicts are unchanged; node and triangle counts follow the library. */
+void orc_scene_set_walls(orc_scene *s, const int32_t *tris, const int32_t *counts);
 /* replace the tree (same format as orc_scene_get_tree); 0 on success */
 int orc_scene_set_tree(orc_scene *s, const uint32_t *children, const float *split,
                        int64_t nnodes, const int32_t *refs, int64_t nrefs);

@@ -236,3 +236,38 @@ def test_bad_inputs_are_rejected(host_ctx, vlib):
     h = C.c_void_p()
     assert vlib.vrg_ctx_create(0, None) == -1
     assert vlib.vrg_env_create(None, C.byref(h)) == -1
+
+
+def test_wall_slots_and_their_shortcut_keep_the_verdicts(oracle, host_ctx):
+    # the room's opaque walls and floor fill the wall slots (the sky ceiling
+    # does not); shadow lines that test them before walking get the same
+    # verdicts, bit for bit, with fewer nodes walked
+    from vrad_gb300 import scenes
+
+    lit = small_lit_scene(96, seed=7)
+    env = _env(host_ctx, lit.xyz, lit.ids)
+    env.set_faces(lit)
+    tris, counts = env.wall_slots()
+    assert counts.tolist() == [2, 2, 2, 2, 2, 0]  # x min/max, y min/max, z min (floor), z max (sky)
+    for f in range(5):
+        a, side = divmod(f, 2)
+        for t in tris[f, :2]:
+            v = lit.xyz[t].reshape(3, 3)
+            assert (v[:, a] == (scenes.ROOM if side else 0.0)).all()
+            assert lit.ids[t] & scenes.TRACE_ID_SKY == 0
+    s = oracle.Scene(lit.xyz, lit.ids)
+    lights = oracle.make_lights(lit.lights)
+    ref, rays, st0 = oracle.gather_luxels(s, lights, len(lit.lights), lit, 0, lit.n_faces, ss=4,
+                                          seed=3, threads=16, stats=True)
+    s.set_walls(tris, counts)
+    got, rays2, st1 = oracle.gather_luxels(s, lights, len(lit.lights), lit, 0, lit.n_faces, ss=4,
+                                           seed=3, threads=16, stats=True)
+    assert rays == rays2 and bits_equal(got, ref)
+    assert st1[1] < 0.8 * st0[1]  # kd nodes
+    # arbitrary lines through the room, through its walls and out of it
+    rng = np.random.default_rng(4)
+    a = rng.uniform(1, 4095, (20000, 3)).astype(np.float32)
+    b = (a + rng.normal(0, 6000, (20000, 3))).astype(np.float32)
+    f_walls = s.test_lines(a, b, threads=16)
+    s.set_walls()
+    assert np.array_equal(f_walls, s.test_lines(a, b, threads=16))

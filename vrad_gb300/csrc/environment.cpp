@@ -160,18 +160,57 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         }
     }
     env->ntop = (uint32_t)top.size();
-    const size_t nr1 = nr ? nr : 1;
-    std::vector<float4> leaf(3 * nr1, make_float4(0, 0, 0, 0));
-    for (size_t r = 0; r < nr; r++) {
-        const TriRecord &t = env->tri_records[wt.refs[r]];
+    // wall slots: per face of the scene box, the largest opaque triangles
+    // lying in that face (a closed room's walls and floor), appended after
+    // the leaf entries so that a shadow line can test the face it leaves
+    // through before walking
+    std::vector<int32_t> wall[6];
+    {
+        std::vector<std::pair<double, int32_t>> cand[6];
+        for (int64_t t = 0; t < n; t++) {
+            if (env->ids[t] & VRG_TRACE_ID_SKY) continue;
+            const float *v = &env->xyz[9 * t];
+            for (int a = 0; a < 3; a++)
+                for (int side = 0; side < 2; side++) {
+                    const float bound = side ? env->max_bound[a] : env->min_bound[a];
+                    if (v[a] != bound || v[3 + a] != bound || v[6 + a] != bound) continue;
+                    double e1[3], e2[3];
+                    for (int c = 0; c < 3; c++) {
+                        e1[c] = (double)v[3 + c] - v[c];
+                        e2[c] = (double)v[6 + c] - v[c];
+                    }
+                    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                                 cz = e1[0] * e2[1] - e1[1] * e2[0];
+                    cand[2 * a + side].push_back({-(cx * cx + cy * cy + cz * cz), (int32_t)t});
+                }
+        }
+        for (int f = 0; f < 6; f++) {
+            std::sort(cand[f].begin(), cand[f].end());
+            for (size_t i = 0; i < cand[f].size() && (int)i < kWallSlots; i++) wall[f].push_back(cand[f][i].second);
+        }
+    }
+    const size_t ne = nr + 6 * (size_t)kWallSlots;  // leaf entries + wall slots
+    std::vector<float4> leaf(3 * ne, make_float4(0, 0, 0, 0));
+    auto put = [&](size_t r, int32_t tri) {
+        const TriRecord &t = env->tri_records[tri];
         float id_bits, idx_bits;
         memcpy(&id_bits, &t.id, 4);
         memcpy(&idx_bits, &t.idx_drop, 4);
         leaf[r] = make_float4(t.nx, t.ny, t.nz, t.d);
         // edge part as pairs (e0, e3) (e1, e4) (e2, e5): b0 and b1 side by side
-        leaf[nr1 + 2 * r] = make_float4(t.e0, t.e3, t.e1, t.e4);
-        leaf[nr1 + 2 * r + 1] = make_float4(t.e2, t.e5, id_bits, idx_bits);
+        leaf[ne + 2 * r] = make_float4(t.e0, t.e3, t.e1, t.e4);
+        leaf[ne + 2 * r + 1] = make_float4(t.e2, t.e5, id_bits, idx_bits);
+    };
+    g.wall_base = (uint32_t)nr;
+    g.wall_count = 0;
+    for (int f = 0; f < 6; f++) {
+        for (int i = 0; i < kWallSlots; i++)
+            env->wall_tris[kWallSlots * f + i] = i < (int)wall[f].size() ? wall[f][i] : -1;
+        env->wall_counts[f] = (int32_t)wall[f].size();
+        for (size_t i = 0; i < wall[f].size(); i++) put(nr + (size_t)kWallSlots * f + i, wall[f][i]);
+        g.wall_count |= (uint32_t)wall[f].size() << (3 * f);
     }
+    for (size_t r = 0; r < nr; r++) put(r, wt.refs[r]);
     env->built = true;
     if (ctx->host_only) return VRG_OK;
     VRG_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -237,6 +276,13 @@ int vrg_env_set_walk_tree_costs(vrg_env *env, float traversal, float intersectio
     env->walk_costs.intersection = intersection;
     env->walk_costs.empty_bonus = empty_bonus;
     env->walk_costs.max_depth = max_depth;
+    return VRG_OK;
+}
+
+int vrg_env_wall_slots(const vrg_env *env, int32_t *tris, int32_t *counts) {
+    if (!env || !env->built) return VRG_ERR_STATE;
+    if (tris) memcpy(tris, env->wall_tris, sizeof env->wall_tris);
+    if (counts) memcpy(counts, env->wall_counts, sizeof env->wall_counts);
     return VRG_OK;
 }
 

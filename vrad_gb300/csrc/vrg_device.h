@@ -28,12 +28,18 @@ struct alignas(16) TriRecord {
 };
 static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
 
+// Wall slots: per face of the scene box (2 * axis + 1 for the max side), up
+// to kWallSlots opaque triangles lying in that face, as extra leaf records.
+constexpr int kWallSlots = 4;
+
 struct SceneGeom {
     float bmin[3], bmax[3];  // root bounds (CalculateTriangleListBounds)
     float smin[3], smax[3];  // bounds of TRACE_ID_SKY triangles
     float scale;             // largest |coordinate| of any vertex
     int32_t has_sky;
     int64_t ntris;
+    uint32_t wall_count;     // 3 bits per box face: its wall slots in use
+    uint32_t wall_base;      // leaf-record index of face 0's first wall slot
 };
 
 // Device view of a resident scene.  The triangle records of the leaves are

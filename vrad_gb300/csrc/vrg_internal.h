@@ -129,6 +129,8 @@ struct vrg_env {
     HostTree tree;        // the reference's tree, built on first request
     bool ref_tree_built = false;
     HostTree walk_tree;   // the tree the device walks (build_walk_tree)
+    int32_t wall_tris[6 * vrg::kWallSlots];  // wall slots per scene-box face (-1: unused)
+    int32_t wall_counts[6] = {0, 0, 0, 0, 0, 0};
     WalkTreeCosts walk_costs;
     std::vector<vrg::TriRecord> tri_records;  // per triangle, insertion order
     vrg::SceneGeom geom{};                     // bounds, sky box, scale

@@ -413,10 +413,54 @@ __device__ __forceinline__ bool line_verdict(const DevScene &s, const LinePlan &
     return (__ldg(&s.tri_ids[h]) & kTraceIdSky) == 0;
 }
 
+// Face of the scene box (padded by `pad`) through which the ray leaves it,
+// 2 * axis + 1 for a max side, and the t there (approximate arithmetic).
+__device__ __forceinline__ int exit_face(const SceneGeom &g, const Ray &ray, const RayPre &rp, float pad,
+                                         float &tex) {
+    const float o[3] = {ray.ox, ray.oy, ray.oz};
+    int f = 0;
+    tex = kInf;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const bool neg = (rp.neg >> a) & 1u;
+        const float t = ((neg ? g.bmin[a] - pad : g.bmax[a] + pad) - o[a]) * rp.inv[a];
+        if (t < tex) {
+            tex = t;
+            f = 2 * a + (neg ? 0 : 1);
+        }
+    }
+    return f;
+}
+
+// True when an opaque triangle lying in the face of the scene box through
+// which the line leaves (a closed room's wall or floor, held in the wall
+// slots) is hit before any_limit by the exact triangle test.  The walk's
+// verdict is then "occluded" whatever lies in front of that wall: the walk
+// would find this hit or stop at an earlier one before any_limit, and no
+// sky triangle can be hit before any_limit.  False says nothing.
+template <int OPT = 0>
+__device__ __forceinline__ bool wall_occludes(const DevScene &s, const LinePlan &p, int32_t skip) {
+    if (s.g.wall_count == 0) return false;
+    float tex;
+    const int f = exit_face(s.g, p.ray, p.rp, p.slack, tex);
+    if (!(tex < 2.0f * p.len)) return false;  // the line ends well inside the box
+    const uint32_t cnt = (s.g.wall_count >> (3 * f)) & 7u;
+    int32_t best = -1;
+    float best_t = kInf;
+    for (uint32_t i = 0; i < cnt; i++) {
+        const size_t k = (size_t)s.g.wall_base + (size_t)kWallSlots * f + i;
+        if (tri_test<kSkyOcc, OPT>(s, p.ray, 0.0f, p.len, skip, p.any_limit, __ldg(s.leaf_planes + k), k,
+                                   best, best_t))
+            return true;
+    }
+    return false;
+}
+
 template <int OPT = 0>
 __device__ __forceinline__ bool line_occluded(const DevScene &s, const Line &L, int32_t skip) {
     const LinePlan p = plan_line(s, L);
     if (p.trivial) return false;
+    if (wall_occludes<OPT>(s, p, skip)) return true;
     float th;
     const int32_t h =
         kd_trace<kSkyOcc, OPT>(s, p.ray, p.rp, p.slack, 0.0f, p.len, skip, p.any_limit, &th);

@@ -224,6 +224,14 @@ class Environment:
                   "get_walk_tree")
         return ch, sp, refs[: nr.value], ht.value
 
+    def wall_slots(self):
+        """(tris (6, 4), counts (6,)): the opaque triangles in each scene-box
+        face that shadow lines test before walking."""
+        tris = np.zeros(24, np.int32)
+        counts = np.zeros(6, np.int32)
+        self._chk(self.lib.vrg_env_wall_slots(self.h, _p(tris), _p(counts)), "wall_slots")
+        return tris.reshape(6, 4), counts
+
     def GetTriangle(self, index) -> bytes:
         buf = (C.c_uint8 * 48)()
         self._chk(self.lib.vrg_env_get_triangle(self.h, index, buf), "GetTriangle")
