@@ -107,3 +107,31 @@ def test_transfer_variants_identical(gpu_ctx, tmp_path):
             continue
         assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
         assert bits_equal(got[2], ref[2])
+
+
+@pytest.mark.gpu
+def test_bounce_variants_identical(gpu_ctx, tmp_path):
+    # 4, 8 or 2 entries per lane per round sum the same entries in the same
+    # order with fused multiply-adds: identical totals
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Context, Environment
+
+    lit = small_lit_scene(240, seed=4)
+    env = Environment(gpu_ctx)
+    env.add_triangles(lit.xyz, lit.ids)
+    env.SetupAccelerationStructure()
+    env.set_faces(lit)
+    env.set_lights(lit.lights)
+    nl = env.make_patches()["n_leaves"]
+    nnz = env.make_transfers(scenes.transfer_directions(1024))
+    env.gather_patch_direct(nl)
+    key = Context.tune_key("bounce_spmv", nnz, nl)
+    outs = []
+    for v in range(3):
+        _force(gpu_ctx, tmp_path, key, v)
+        total, bounces, _ = env.bounce_light(nl, max_bounces=12, rel_tol=0.0)
+        assert bounces == 12
+        outs.append(total)
+    assert np.abs(outs[0]).max() > 0
+    for o in outs[1:]:
+        assert bits_equal(o, outs[0])

@@ -175,7 +175,8 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
     using SpmvKernel = void (*)(const int64_t *, const int32_t *, const float *, const float4 *,
                                 float4 *, float4 *, const LeafInfo *, int64_t,
                                 const BounceControl *, double *);
-    const SpmvKernel kvar[3] = {k_bounce_spmv<4>, k_bounce_spmv<8>, k_bounce_spmv<2>};
+    constexpr int kSpmvVariants = 3;
+    const SpmvKernel kvar[kSpmvVariants] = {k_bounce_spmv<4>, k_bounce_spmv<8>, k_bounce_spmv<2>};
     auto spmv_blocks = [&](int v) {
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kvar[v], kSpmvThreads, 0) != cudaSuccess ||
@@ -197,7 +198,7 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
     int var = 0;
     if (n > 0 && max_bounces > 0) {
         bool ran = false;
-        const int rc = tune_pick(ctx, tune_key("bounce_spmv", env->nnz, n), 3,
+        const int rc = tune_pick(ctx, tune_key("bounce_spmv", env->nnz, n), kSpmvVariants,
                                  [&](int v) { ran = true; return spmv(v, e0, e1); }, &var);
         if (rc != VRG_OK) return rc;
         if (ran) VRG_CUDA(ctx, init());  // tuning ran bounces: start over

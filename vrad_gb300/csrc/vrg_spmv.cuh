@@ -9,8 +9,8 @@
 namespace vrg {
 
 // sum_j w_j * x[col_j] over the row's entries [b, e) for one warp: lane l
-// takes entries b+l, b+l+32, ... in that order (so every U gives the same
-// per-lane sums), U of them per round, with the next round's column and
+// takes entries b+l, b+l+32, ... in that order, each added with one fused
+// multiply-add (so every U gives the same per-lane sums), U of them per round, with the next round's column and
 // weight loads in flight while this round's x entries are gathered (the
 // gathers wait on the column loads; without the overlap every round pays
 // both latencies back to back).  Returns the lane's partial sums; the
@@ -47,9 +47,9 @@ __device__ __forceinline__ float3 row_gather(const int32_t *__restrict__ col,
         for (int k = 0; k < U; k++) xv[k] = __ldg(x + c[k]);
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            ar += wv[k] * xv[k].x;
-            ag += wv[k] * xv[k].y;
-            ab += wv[k] * xv[k].z;
+            ar = __fmaf_rn(wv[k], xv[k].x, ar);
+            ag = __fmaf_rn(wv[k], xv[k].y, ag);
+            ab = __fmaf_rn(wv[k], xv[k].z, ab);
         }
 #pragma unroll
         for (int k = 0; k < U; k++) {
@@ -60,9 +60,9 @@ __device__ __forceinline__ float3 row_gather(const int32_t *__restrict__ col,
     for (; i < e; i += 32) {
         const float wk = __ldg(w + i);
         const float4 xk = __ldg(x + __ldg(col + i));
-        ar += wk * xk.x;
-        ag += wk * xk.y;
-        ab += wk * xk.z;
+        ar = __fmaf_rn(wk, xk.x, ar);
+        ag = __fmaf_rn(wk, xk.y, ag);
+        ab = __fmaf_rn(wk, xk.z, ab);
     }
     return make_float3(ar, ag, ab);
 }
