@@ -224,11 +224,28 @@ def run_gpu(args, rank, world, local_rank):
         lib_ctx.autotune_load(args.autotune_file)
     lib = lib_ctx.lib
 
+    def admit(xyz, ids):
+        """The scene's environment, and the time SetupAccelerationStructure
+        takes with the walk tree built on the GPU and on the host (ms; the
+        GPU build is timed after a first one that loads its kernels)."""
+        times = {}
+        for on_device in (1, 0, 1):
+            e = Environment(lib_ctx)
+            e.set_walk_tree_builder(on_device)
+            e.add_triangles(xyz, ids)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e.SetupAccelerationStructure()
+            times["device" if on_device else "host"] = round((time.perf_counter() - t0) * 1e3, 2)
+            e.close()
+        e = Environment(lib_ctx)  # the default builder for this size
+        e.add_triangles(xyz, ids)
+        e.SetupAccelerationStructure()
+        return e, times
+
     if args.workload == "anyhit":
         sc = scenes.anyhit_scene(SEED)
-        env = Environment(lib_ctx)
-        env.add_triangles(sc.xyz, sc.ids)
-        env.SetupAccelerationStructure()
+        env, admit_ms = admit(sc.xyz, sc.ids)
         n = sc.starts.shape[0]
         d_a = torch.from_numpy(sc.starts).to(dev)
         d_b = torch.from_numpy(sc.stops).to(dev)
@@ -255,9 +272,7 @@ def run_gpu(args, rank, world, local_rank):
         bytes_per_unit = None
     else:
         lit = scenes.lit_scene(SEED, n_faces=args.faces)
-        env = Environment(lib_ctx)
-        env.add_triangles(lit.xyz, lit.ids)
-        env.SetupAccelerationStructure()
+        env, admit_ms = admit(lit.xyz, lit.ids)
         env.set_faces(lit)
         lights = light_array(lit.lights)
         env.set_lights(lit.lights)
@@ -410,7 +425,8 @@ def run_gpu(args, rank, world, local_rank):
                       {"luxel_samples_per_s_M": round(4 * nlux * args.steps * world / (total_ms * 1e-3) / 1e6, 3)}),
                    "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",
                    "autotune": {"bucket": tkey, "variant": tv,
-                                "variant_ms": [round(x, 4) for x in tms]}},
+                                "variant_ms": [round(x, 4) for x in tms]},
+                   "setup_acceleration_structure_ms": admit_ms},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

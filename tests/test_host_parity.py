@@ -136,6 +136,9 @@ def test_walk_tree_costs_are_checked(host_ctx, anyhit_scene):
         env.set_walk_tree_costs(max_depth=32)
     with pytest.raises(VrgError):
         env.set_walk_tree_costs(empty_bonus=1.5)
+    with pytest.raises(VrgError):
+        env.set_walk_tree_builder(2)
+    env.set_walk_tree_builder(1)  # a host-only context still builds on the host
     env.set_walk_tree_costs(1.0, 1.5, 0.9, 20)
     env.add_triangles(anyhit_scene.xyz[:600], anyhit_scene.ids[:600])
     env.SetupAccelerationStructure()

@@ -50,6 +50,7 @@ SIGNATURES = {
     "vrg_env_get_tree": (C.c_int, [P, P, P, P]),
     "vrg_env_set_walk_tree_costs": (C.c_int, [P, F, F, F, I32]),
     "vrg_env_walk_tree_info": (C.c_int, [P, P, P, P]),
+    "vrg_env_set_walk_tree_builder": (C.c_int, [P, I32]),
     "vrg_env_wall_slots": (C.c_int, [P, P, P]),
     "vrg_env_get_walk_tree": (C.c_int, [P, P, P, P]),
     "vrg_env_get_triangle": (C.c_int, [P, I64, P]),

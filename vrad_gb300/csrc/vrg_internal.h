@@ -132,6 +132,7 @@ struct vrg_env {
     int32_t wall_tris[6 * vrg::kWallSlots];  // wall slots per scene-box face (-1: unused)
     int32_t wall_counts[6] = {0, 0, 0, 0, 0, 0};
     WalkTreeCosts walk_costs;
+    int walk_builder = -1;  // walk tree: 0 host (full sweep), 1 GPU (binned), -1 by size
     std::vector<vrg::TriRecord> tri_records;  // per triangle, insertion order
     vrg::SceneGeom geom{};                     // bounds, sky box, scale
 
@@ -224,6 +225,7 @@ void scene_bounds(const std::vector<float> &xyz, float *mn, float *mx);
 void build_kd_tree(const std::vector<float> &xyz, HostTree &tree, float *mn, float *mx);
 void build_walk_tree(const std::vector<float> &xyz, const float *mn, const float *mx,
                      const WalkTreeCosts &cost, HostTree &tree);
+int build_walk_tree_device(vrg_env *env, HostTree &tree);  // kdbuild_gpu.cu
 void light_set_falloff(const vrg_light_keys &k, vrg_light &l);
 void light_parse_spot(const vrg_light_keys &k, vrg_light &l);
 int make_rect_patches(const vrg_env &env, float max_chop, float min_chop, PatchSet &out);

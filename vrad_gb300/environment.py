@@ -212,6 +212,11 @@ class Environment:
                                                        empty_bonus, max_depth),
                   "set_walk_tree_costs")
 
+    def set_walk_tree_builder(self, mode):
+        """0 / False: host, 1 / True: GPU, -1: by scene size (the default)."""
+        self._chk(self.lib.vrg_env_set_walk_tree_builder(self.h, int(mode)),
+                  "set_walk_tree_builder")
+
     def walk_tree(self):
         """The tree the device walks: (children, split, refs, height)."""
         nn, nr, ht = C.c_int64(), C.c_int64(), C.c_int32()
