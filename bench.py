@@ -344,6 +344,36 @@ def run_gpu(args, rank, world, local_rank):
         e2e_t.append(time.perf_counter() - t0)
     e2e_value = units * world / statistics.mean(e2e_t) / 1e6
 
+    closest = None
+    if args.workload == "anyhit":
+        # the same lines with the closest hit's triangle and distance written
+        # too (Trace4Rays semantics over the normalised segments)
+        d_h = torch.empty(n, dtype=torch.int32, device=dev)
+        d_t = torch.empty(n, dtype=torch.float32, device=dev)
+
+        def step_hit():
+            rc = lib.vrg_env_occlusion_mask_d(env.h, d_a.data_ptr(), d_b.data_ptr(), n, -1,
+                                              d_m.data_ptr(), d_h.data_ptr(), d_t.data_ptr())
+            assert rc == 0, rc
+
+        for _ in range(max(args.warmup, 3)):
+            step_hit()
+            flush.zero_()
+        torch.cuda.synchronize()
+        cts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_ev.record(stream)
+            step_hit()
+            b_ev.record(stream)
+            torch.cuda.synchronize()
+            cts.append(a_ev.elapsed_time(b_ev))
+        hv, hms = lib_ctx.autotune_choice(Context.tune_key("trace_mask_hit", env.num_triangles(), n))
+        closest = {"value": round(n / (statistics.mean(cts) * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+                   "ms_per_step": round(statistics.mean(cts), 4), "outputs": "mask + hit index + t",
+                   "autotune": {"variant": hv, "variant_ms": [round(x, 4) for x in hms]}}
+
     if rank != 0:
         if dist:
             td.destroy_process_group()
@@ -427,6 +457,7 @@ def run_gpu(args, rank, world, local_rank):
                    "autotune": {"bucket": tkey, "variant": tv,
                                 "variant_ms": [round(x, 4) for x in tms]},
                    "setup_acceleration_structure_ms": admit_ms},
+        **({"closest_hit": closest} if closest else {}),
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
