@@ -10,7 +10,10 @@
  * Ownership: host buffers belong to the caller and are only borrowed for the
  * duration of the call.  Device memory is owned by the handle that created
  * it.  Functions ending in _d take device pointers; all others take host
- * pointers and copy through pinned staging inside the call.
+ * pointers.  The trace entry points (vrg_env_occlusion_mask,
+ * vrg_env_trace_closest, vrg_env_test_line_does_hit_sky) read page-locked
+ * host inputs (cudaHostAlloc / cudaHostRegister) in place over the CPU-GPU
+ * link; other host buffers are copied in and out inside the call.
  *
  * Threading: a context may be shared by several host threads; each
  * environment serialises its own calls with a mutex.

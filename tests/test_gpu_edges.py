@@ -79,3 +79,51 @@ def test_relight_without_change_keeps_the_bake(gpu_ctx):
     err = np.abs(after["patch_total"] - before["patch_total"]) / np.maximum(
         np.abs(before["patch_total"]), 1e-6 * scale)
     assert err.max() <= 1e-3
+
+
+def test_page_locked_inputs_are_read_in_place(env_and_oracle, anyhit_scene):
+    # page-locked end points go to the walk without a copy; the answers are
+    # those of pageable inputs (which are copied first)
+    import ctypes as C
+
+    import torch
+
+    env, _ = env_and_oracle
+    n = 50000
+    a, b = anyhit_scene.starts[:n], anyhit_scene.stops[:n]
+    want = env.occlusion_mask(a, b, closest=True)
+    ha = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    hb = torch.from_numpy(np.ascontiguousarray(b)).pin_memory()
+    mask = np.zeros((n + 31) // 32, np.uint32)
+    hit = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    rc = env.lib.vrg_env_occlusion_mask(env.h, C.c_void_p(ha.data_ptr()), C.c_void_p(hb.data_ptr()), n,
+                                        -1, mask.ctypes.data, hit.ctypes.data, t.ctypes.data)
+    assert rc == 0
+    assert np.array_equal(mask, want[0]) and np.array_equal(hit, want[1]) and bits_equal(t, want[2])
+
+
+def test_page_locked_rays_and_lines(env_and_oracle, anyhit_scene):
+    import ctypes as C
+
+    import torch
+
+    env, _ = env_and_oracle
+    n = 20000
+    a, b = anyhit_scene.starts[:n], anyhit_scene.stops[:n]
+    d = (b - a).astype(np.float32)
+    ln = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]).astype(np.float32)
+    dn = (d * (np.float32(1.0) / ln)[:, None]).astype(np.float32)
+    want_h, want_t = env.trace_closest(a, dn, 0.0, ln)
+    want_f = env.test_line_does_hit_sky(a, b)
+    pin = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+           for x in (a, dn, np.zeros(n, np.float32), ln, b)]
+    hit = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    frac = np.empty(n, np.float32)
+    p = [C.c_void_p(x.data_ptr()) for x in pin]
+    assert env.lib.vrg_env_trace_closest(env.h, p[0], p[1], p[2], p[3], n, -1, hit.ctypes.data,
+                                         t.ctypes.data) == 0
+    assert env.lib.vrg_env_test_line_does_hit_sky(env.h, p[0], p[4], n, -1, frac.ctypes.data) == 0
+    assert np.array_equal(hit, want_h) and bits_equal(t, want_t)
+    assert np.array_equal(frac, want_f)

@@ -96,6 +96,19 @@ int upload(vrg_ctx *ctx, DevBuf &buf, const void *src, size_t bytes) {
     return VRG_OK;
 }
 
+// The device's address of a host buffer that is page-locked (cudaHostAlloc,
+// cudaHostRegister, a pinned torch tensor): kernels read it in place, over
+// the CPU-GPU link, instead of waiting for a copy.  NULL for any other
+// memory (pageable buffers are copied).
+const void *pinned_view(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int download(vrg_ctx *ctx, void *dst, const DevBuf &buf, size_t bytes) {
     if (bytes) VRG_CUDA(ctx, cudaMemcpyAsync(dst, buf.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     return VRG_OK;
@@ -312,15 +325,25 @@ int vrg_env_trace_closest(vrg_env *env, const float *orig, const float *dir, con
     if (n == 0) return VRG_OK;
     std::lock_guard<std::mutex> lk(env->mu);
     vrg_ctx *ctx = env->ctx;
-    TRY(upload(ctx, env->d_in0, orig, 12 * n));
-    TRY(upload(ctx, env->d_in1, dir, 12 * n));
-    VRG_CUDA(ctx, env->d_out2.reserve(8 * n));
-    VRG_CUDA(ctx, cudaMemcpyAsync(env->d_out2.as<float>(), tmin, 4 * n, cudaMemcpyHostToDevice, ctx->stream));
-    VRG_CUDA(ctx, cudaMemcpyAsync(env->d_out2.as<float>() + n, tmax, 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+    // page-locked inputs are read in place, others copied first
+    const float *d_orig = static_cast<const float *>(pinned_view(orig));
+    const float *d_dir = static_cast<const float *>(pinned_view(dir));
+    const float *d_tmin = static_cast<const float *>(pinned_view(tmin));
+    const float *d_tmax = static_cast<const float *>(pinned_view(tmax));
+    if (!d_orig || !d_dir || !d_tmin || !d_tmax) {
+        TRY(upload(ctx, env->d_in0, orig, 12 * n));
+        TRY(upload(ctx, env->d_in1, dir, 12 * n));
+        VRG_CUDA(ctx, env->d_out2.reserve(8 * n));
+        VRG_CUDA(ctx, cudaMemcpyAsync(env->d_out2.as<float>(), tmin, 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+        VRG_CUDA(ctx, cudaMemcpyAsync(env->d_out2.as<float>() + n, tmax, 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+        d_orig = env->d_in0.as<float>();
+        d_dir = env->d_in1.as<float>();
+        d_tmin = env->d_out2.as<float>();
+        d_tmax = env->d_out2.as<float>() + n;
+    }
     VRG_CUDA(ctx, env->d_out0.reserve(4 * n));
     VRG_CUDA(ctx, env->d_out1.reserve(4 * n));
-    TRY(launch_trace_closest(env, env->d_in0.as<float>(), env->d_in1.as<float>(), env->d_out2.as<float>(),
-                             env->d_out2.as<float>() + n, n, skip_id, env->d_out0.as<int32_t>(),
+    TRY(launch_trace_closest(env, d_orig, d_dir, d_tmin, d_tmax, n, skip_id, env->d_out0.as<int32_t>(),
                              env->d_out1.as<float>()));
     TRY(download(ctx, out_hit, env->d_out0, 4 * n));
     TRY(download(ctx, out_t, env->d_out1, 4 * n));
@@ -367,14 +390,22 @@ int vrg_env_occlusion_mask(vrg_env *env, const float *start, const float *stop, 
     vrg_ctx *ctx = env->ctx;
     const bool want = out_hit && out_t;
     const int64_t words = (n + 31) / 32;
-    TRY(upload(ctx, env->d_in0, start, 12 * n));
-    TRY(upload(ctx, env->d_in1, stop, 12 * n));
+    // page-locked end points are read where they are (the walk reads each
+    // line's 24 bytes once, as it takes the line); others are copied first
+    const float *d_start = static_cast<const float *>(pinned_view(start));
+    const float *d_stop = static_cast<const float *>(pinned_view(stop));
+    if (!d_start || !d_stop) {
+        TRY(upload(ctx, env->d_in0, start, 12 * n));
+        TRY(upload(ctx, env->d_in1, stop, 12 * n));
+        d_start = env->d_in0.as<float>();
+        d_stop = env->d_in1.as<float>();
+    }
     VRG_CUDA(ctx, env->d_out2.reserve(4 * words));
     if (want) {
         VRG_CUDA(ctx, env->d_out0.reserve(4 * n));
         VRG_CUDA(ctx, env->d_out1.reserve(4 * n));
     }
-    TRY(launch_occlusion_mask(env, env->d_in0.as<float>(), env->d_in1.as<float>(), n, skip_id,
+    TRY(launch_occlusion_mask(env, d_start, d_stop, n, skip_id,
                               env->d_out2.as<uint32_t>(), want ? env->d_out0.as<int32_t>() : nullptr,
                               want ? env->d_out1.as<float>() : nullptr));
     TRY(download(ctx, out_mask, env->d_out2, 4 * words));
@@ -394,10 +425,16 @@ int vrg_env_test_line_does_hit_sky(vrg_env *env, const float *start, const float
     vrg_ctx *ctx = env->ctx;
     // testline.go:36: skip id = TRACE_ID_STATICPROP | staticPropToSkip
     const int32_t skip = VRG_TRACE_ID_STATICPROP | static_prop_to_skip;
-    TRY(upload(ctx, env->d_in0, start, 12 * n));
-    TRY(upload(ctx, env->d_in1, stop, 12 * n));
+    const float *d_start = static_cast<const float *>(pinned_view(start));
+    const float *d_stop = static_cast<const float *>(pinned_view(stop));
+    if (!d_start || !d_stop) {
+        TRY(upload(ctx, env->d_in0, start, 12 * n));
+        TRY(upload(ctx, env->d_in1, stop, 12 * n));
+        d_start = env->d_in0.as<float>();
+        d_stop = env->d_in1.as<float>();
+    }
     VRG_CUDA(ctx, env->d_out0.reserve(4 * n));
-    TRY(launch_test_lines(env, env->d_in0.as<float>(), env->d_in1.as<float>(), n, skip, env->d_out0.as<float>()));
+    TRY(launch_test_lines(env, d_start, d_stop, n, skip, env->d_out0.as<float>()));
     TRY(download(ctx, fraction_visible, env->d_out0, 4 * n));
     return sync(ctx);
 }
