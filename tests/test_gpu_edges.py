@@ -127,3 +127,30 @@ def test_page_locked_rays_and_lines(env_and_oracle, anyhit_scene):
     assert env.lib.vrg_env_test_line_does_hit_sky(env.h, p[0], p[4], n, -1, frac.ctypes.data) == 0
     assert np.array_equal(hit, want_h) and bits_equal(t, want_t)
     assert np.array_equal(frac, want_f)
+
+
+def test_wall_slots_respect_the_skip_id(gpu_ctx, oracle):
+    # a room whose walls are one static prop: skipping that prop lets lines
+    # through the walls (the wall test must skip them as the walk does)
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    prop = scenes.TRACE_ID_STATICPROP | 5
+    soup = scenes.TriangleSoup()
+    soup.add_box(prop, (0.0, 0.0, 0.0), (scenes.ROOM,) * 3, ceiling_id=scenes.TRACE_ID_SKY)
+    soup.add_box(scenes.TRACE_ID_OPAQUE, (1000.0, 1000.0, 1000.0), (1500.0, 1500.0, 1500.0))
+    xyz, ids = soup.arrays()
+    env = Environment(gpu_ctx)
+    env.add_triangles(xyz, ids)
+    env.SetupAccelerationStructure()
+    tris, counts = env.wall_slots()
+    assert counts[:5].tolist() == [2, 2, 2, 2, 2] and counts[5] == 0
+    rng = np.random.default_rng(8)
+    a = rng.uniform(1, 4095, (20000, 3)).astype(np.float32)
+    b = (a + rng.normal(0, 8000, (20000, 3))).astype(np.float32)  # most leave the room
+    s = oracle.Scene(xyz, ids)
+    for skip_prop in (-1, 5):
+        got = env.test_line_does_hit_sky(a, b, skip_prop)
+        want = s.test_lines(a, b, skip=(prop if skip_prop == 5 else -1), threads=16)
+        assert np.array_equal(got, want)
+    assert (env.test_line_does_hit_sky(a, b, 5) == 1.0).mean() > 0.5
