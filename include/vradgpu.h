@@ -155,7 +155,7 @@ int64_t vrg_env_num_triangles(const vrg_env *env);
 int vrg_env_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height);
 /* OptimizedKDTree (children word, split float) and TriangleIndexList. */
 int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32_t *refs);
-/* SAH costs of the walk tree (defaults 1, 1.5, 0.8, 28): a split costs
+/* SAH costs of the walk tree (defaults 1, 1.2, 0.9, 28): a split costs
  * traversal + intersection * (P_left * N_left + P_right * N_right), times
  * empty_bonus when a side is empty; depth at most max_depth (< 32).  Only
  * before vrg_env_setup_acceleration_structure. */

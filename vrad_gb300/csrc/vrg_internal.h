@@ -95,13 +95,15 @@ struct HostTree {
 };
 
 // SAH costs of the tree the device walks (build_walk_tree).  Measured on
-// the 12,300-triangle any-hit room and the 8,208-triangle direct-light room,
-// intersection costs of 1.5 to 10 give walks within 2 % of each other; 1.5
-// was the fastest for the direct-light gather.
+// the 12,300-triangle any-hit room and the 8,208-triangle direct-light room:
+// intersection costs from 0.8 to 10 and empty-space bonuses from 0.7 to 1
+// give walks within 5 % of each other; 1.2 and 0.9 make the smallest trees
+// that keep the direct-light gather fastest (16.0 ms against 16.6 at 1.5 /
+// 0.8), at 1-2 % of the any-hit walk.
 struct WalkTreeCosts {
     float traversal = 1.0f;
-    float intersection = 1.5f;
-    float empty_bonus = 0.8f;
+    float intersection = 1.2f;
+    float empty_bonus = 0.9f;
     int max_depth = 28;  // below the traversal stack (kStackMax)
 };
 

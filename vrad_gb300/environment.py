@@ -206,7 +206,7 @@ class Environment:
         self._chk(self.lib.vrg_env_get_tree(self.h, _p(ch), _p(sp), _p(refs)), "get_tree")
         return ch, sp, refs[: nr.value], ht.value
 
-    def set_walk_tree_costs(self, traversal=1.0, intersection=1.5, empty_bonus=0.8,
+    def set_walk_tree_costs(self, traversal=1.0, intersection=1.2, empty_bonus=0.9,
                             max_depth=28):
         self._chk(self.lib.vrg_env_set_walk_tree_costs(self.h, traversal, intersection,
                                                        empty_bonus, max_depth),
