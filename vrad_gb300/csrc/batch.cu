@@ -84,7 +84,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_batch_gather(
             const int sg = upper_segment(seg, 2 * nscenes, gi);
             const int64_t local = gi - __ldg(seg + sg);
             const BatchDesc *d = descs + (sg < nscenes ? sg : sg - nscenes);
-            const DevScene &scene = d->scene;
+            // the item's point and normal, then one gather_point call site
+            // (a second inlined copy of the gather costs through code size)
+            float px, py, pz, nx, ny, nz;
             if (sg < nscenes) {
                 luxel_item = true;
                 lux = local / ss;
@@ -94,15 +96,22 @@ __global__ void __launch_bounds__(kThreads, 8) k_batch_gather(
                 int iu, iv;  // the face's luxels in 4 x 2 tiles
                 tile_luxel(lux - __ldg(d->luxel_off + f), fr.nu, fr.nv, iu, iv);
                 lux = __ldg(d->luxel_off + f) + (int64_t)iv * fr.nu + iu;
-                float px, py, pz;
                 luxel_sample(fr, lux, iu, iv, k, ss, seed, px, py, pz);
-                gather_point<kSkyTrace>(scene, d->lights, d->nl, px, py, pz, fr.normal.x, fr.normal.y, fr.normal.z,
-                             r, g, b, rays);
+                nx = fr.normal.x;
+                ny = fr.normal.y;
+                nz = fr.normal.z;
                 lux_out = d->out_rgb;
             } else {
                 const float *p = d->ppts + 3 * local, *n = d->pnrm + 3 * local;
-                gather_point<kSkyTrace>(scene, d->lights, d->nl, __ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(n),
-                             __ldg(n + 1), __ldg(n + 2), r, g, b, rays);
+                px = __ldg(p);
+                py = __ldg(p + 1);
+                pz = __ldg(p + 2);
+                nx = __ldg(n);
+                ny = __ldg(n + 1);
+                nz = __ldg(n + 2);
+            }
+            gather_point<kSkyTrace>(d->scene, d->lights, d->nl, px, py, pz, nx, ny, nz, r, g, b, rays);
+            if (!luxel_item) {
                 float *o = d->pout + 3 * local;
                 o[0] = r;
                 o[1] = g;
