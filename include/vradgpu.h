@@ -168,10 +168,10 @@ int vrg_env_set_walk_tree_costs(vrg_env *env, float traversal, float intersectio
  * occludes it whatever lies in between, so the walk is skipped. */
 int vrg_env_wall_slots(const vrg_env *env, int32_t *tris, int32_t *counts);
 /* Where the walk tree is built: 0 on the host (every extent boundary a
- * candidate plane), 1 on the context's GPU (binned SAH: per axis the first
- * start and last end in each of 256 bins), -1 (default) on the GPU from
- * 65,536 triangles up, else on the host.  A host-only context always builds
- * on the host.  Only before vrg_env_setup_acceleration_structure. */
+ * candidate plane), 1 or -1 (default) on the context's GPU (nodes of up to
+ * 512 triangles weigh every extent boundary, larger ones the first start
+ * and last end in each of 256 bins per axis).  A host-only context always
+ * builds on the host.  Only before vrg_env_setup_acceleration_structure. */
 int vrg_env_set_walk_tree_builder(vrg_env *env, int32_t mode);
 /* The walk tree, in the format of vrg_env_tree_info / vrg_env_get_tree. */
 int vrg_env_walk_tree_info(const vrg_env *env, int64_t *nodes, int64_t *refs, int32_t *height);

@@ -103,7 +103,7 @@ def test_direct_light_on_device_built_tree(gpu_ctx):
 
 
 def test_large_scene_builds_on_the_gpu_by_default(gpu_ctx, oracle):
-    # 72,012 triangles: past the size where the default builder is the GPU's
+    # 72,012 triangles through the default builder (the GPU's)
     from vrad_gb300 import scenes
     from vrad_gb300.environment import Environment
 

@@ -4,15 +4,15 @@
 // Same tree format and the same leaf rule as build_walk_tree (kdbuild.cpp):
 // a triangle goes to the left child when its extent, clamped to the node's
 // box, starts below the split plane, to the right one when it ends above
-// it, and a triangle lying in the plane goes right; so every leaf holds
+// it, and a triangle lying in the plane to the cheaper side; so every leaf holds
 // every triangle touching its cell and the walk's answers are those of
-// brute force, whatever planes are chosen.  The planes differ: instead of
-// every extent boundary, each node weighs, per axis and per each of kBins
-// bins of its box, the first start and the last end of the clamped extents
-// that fall in the bin, with counts from a histogram of the extents (the
-// binned SAH of Wald, "On fast construction of SAH-based bounding volume
-// hierarchies", 2007, applied to kd splits, with planes kept on extent
-// boundaries as the full sweep keeps them).
+// brute force, whatever planes are chosen.  Nodes of up to kSmallNode
+// triangles weigh every extent boundary exactly (choose_exact); larger ones,
+// per axis and per each of kBins bins of their box, the first start and the
+// last end of the clamped extents that fall in the bin, with counts from a
+// histogram of the extents (the binned SAH of Wald, "On fast construction of
+// SAH-based bounding volume hierarchies", 2007, applied to kd splits, with
+// planes kept on extent boundaries as the full sweep keeps them).
 //
 // Level by level, three launches: (1) one block per node bins its
 // triangles, picks a plane or makes it a leaf, and counts the children's
@@ -45,6 +45,7 @@ struct LDec {         // what a node of the level became
     int32_t axis;     // -1: leaf
     float split;
     int32_t nl, nr;
+    int32_t planar_left;  // triangles lying in the plane go left (else right)
 };
 
 struct LScan {        // offsets from the scan
@@ -67,6 +68,89 @@ __device__ __forceinline__ int bin_of(float v, float lo, float inv_w) {
     return b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
 }
 
+// A small node weighs every extent boundary exactly, as the host sweep
+// does: each thread takes candidate planes (the clamped start and end of
+// each triangle on each axis) and counts both sides over the node's list;
+// the block keeps the cheapest (ties to the lower candidate, so the choice
+// is the same on every run).  Triangles lying in the plane go to the side
+// that makes the split cheaper, as in the host sweep.
+constexpr int kSmallNode = 512;
+
+__device__ void choose_exact(const LNode &nd, const int32_t *__restrict__ refs, const float *__restrict__ lo,
+                             const float *__restrict__ hi, int64_t ntri, const WalkTreeCosts &cost,
+                             LDec *__restrict__ out) {
+    __shared__ double bc_s[kBuildThreads];
+    __shared__ int bi_s[kBuildThreads];
+    __shared__ float bp_s[kBuildThreads];
+    __shared__ int bl_s[kBuildThreads], br_s[kBuildThreads];
+    const int n = nd.rcnt, tid = threadIdx.x;
+    const double d0 = (double)nd.mx[0] - nd.mn[0], d1 = (double)nd.mx[1] - nd.mn[1],
+                 d2 = (double)nd.mx[2] - nd.mn[2];
+    const double sa = 2.0 * (d0 * d1 + d0 * d2 + d1 * d2);
+    double bc = (double)cost.intersection * n;
+    int bi = 0x7fffffff, bl = 0, br = 0;
+    float bp = 0.0f;
+    for (int c = tid; c < 6 * n && sa > 0.0; c += blockDim.x) {
+        const int a = c / (2 * n), r = (c % (2 * n)) >> 1;
+        const int32_t t = refs[nd.rbeg + r];
+        const float p = (c & 1) ? fminf(hi[a * ntri + t], nd.mx[a]) : fmaxf(lo[a * ntri + t], nd.mn[a]);
+        if (!(p > nd.mn[a] && p < nd.mx[a])) continue;
+        int cl = 0, cr = 0, np = 0;
+        for (int k = 0; k < n; k++) {
+            const int32_t u = refs[nd.rbeg + k];
+            const float l = fmaxf(lo[a * ntri + u], nd.mn[a]), h = fminf(hi[a * ntri + u], nd.mx[a]);
+            if (l == h && l == p) {
+                np++;
+            } else {
+                cl += l < p;
+                cr += h > p;
+            }
+        }
+        const double da = a == 0 ? d0 : (a == 1 ? d1 : d2);
+        const double db = a == 0 ? d1 : d0, dc = a == 2 ? d1 : d2;
+        const double f = ((double)p - nd.mn[a]) / da;
+        const double sl = 2.0 * (f * da * db + f * da * dc + db * dc);
+        const double sr = 2.0 * ((1.0 - f) * da * db + (1.0 - f) * da * dc + db * dc);
+        for (int side = 0; side < 2; side++) {  // the plane's own triangles left, then right
+            const int l2 = cl + (side == 0 ? np : 0), r2 = cr + (side == 1 ? np : 0);
+            double cst = cost.traversal + cost.intersection * (sl / sa * l2 + sr / sa * r2);
+            if (l2 == 0 || r2 == 0) cst *= cost.empty_bonus;
+            const int ci = 2 * c + side;
+            if (cst < bc || (cst == bc && bi != 0x7fffffff && ci < bi)) {
+                bc = cst;
+                bi = ci;
+                bp = p;
+                bl = l2;
+                br = r2;
+            }
+        }
+    }
+    bc_s[tid] = bc;
+    bi_s[tid] = bi;
+    bp_s[tid] = bp;
+    bl_s[tid] = bl;
+    br_s[tid] = br;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (tid < o) {
+            const double c2 = bc_s[tid + o];
+            const int i2 = bi_s[tid + o];
+            if (c2 < bc_s[tid] || (c2 == bc_s[tid] && i2 < bi_s[tid])) {
+                bc_s[tid] = c2;
+                bi_s[tid] = i2;
+                bp_s[tid] = bp_s[tid + o];
+                bl_s[tid] = bl_s[tid + o];
+                br_s[tid] = br_s[tid + o];
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const int a = bi_s[0] == 0x7fffffff ? -1 : (bi_s[0] >> 1) / (2 * n);
+        *out = a < 0 ? LDec{-1, 0.0f, 0, 0, 0} : LDec{a, bp_s[0], bl_s[0], br_s[0], (bi_s[0] & 1) == 0};
+    }
+}
+
 // (1) bin, choose, count
 __global__ void __launch_bounds__(kBuildThreads) k_kd_choose(
     const LNode *__restrict__ nodes, const int32_t *__restrict__ refs, const float *__restrict__ lo,
@@ -75,12 +159,16 @@ __global__ void __launch_bounds__(kBuildThreads) k_kd_choose(
     __shared__ uint32_t kmin[3][kBins], kmax[3][kBins];  // per bin: first start, last end
     __shared__ double best_c[3];
     __shared__ float best_s[3];
-    __shared__ int cnt[2];
+    __shared__ int cnt[3];
     const LNode nd = nodes[blockIdx.x];
     const int n = nd.rcnt;
     const int tid = threadIdx.x;
     if (n <= 1 || level + 1 >= cost.max_depth) {
-        if (tid == 0) dec[blockIdx.x] = LDec{-1, 0.0f, 0, 0};
+        if (tid == 0) dec[blockIdx.x] = LDec{-1, 0.0f, 0, 0, 0};
+        return;
+    }
+    if (n <= kSmallNode) {
+        choose_exact(nd, refs, lo, hi, ntri, cost, dec + blockIdx.x);
         return;
     }
     for (int i = tid; i < 3 * kBins; i += blockDim.x) {
@@ -147,7 +235,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_kd_choose(
         best_c[a] = bc;
         best_s[a] = bs;
     }
-    if (tid < 2) cnt[tid] = 0;
+    if (tid < 3) cnt[tid] = 0;
     __syncthreads();
     int axis = -1;
     double bc = (double)cost.intersection * n;
@@ -157,16 +245,16 @@ __global__ void __launch_bounds__(kBuildThreads) k_kd_choose(
             axis = a;
         }
     if (axis < 0) {
-        if (tid == 0) dec[blockIdx.x] = LDec{-1, 0.0f, 0, 0};
+        if (tid == 0) dec[blockIdx.x] = LDec{-1, 0.0f, 0, 0, 0};
         return;
     }
     const float s = best_s[axis];
-    int cl = 0, cr = 0;
+    int cl = 0, cr = 0, np = 0;
     for (int r = tid; r < n; r += blockDim.x) {
         const int32_t t = refs[nd.rbeg + r];
         const float l = fmaxf(lo[axis * ntri + t], nd.mn[axis]), h = fminf(hi[axis * ntri + t], nd.mx[axis]);
         if (l == h && l == s) {
-            cr++;
+            np++;
         } else {
             cl += l < s;
             cr += h > s;
@@ -174,6 +262,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_kd_choose(
     }
     atomicAdd(&cnt[0], cl);
     atomicAdd(&cnt[1], cr);
+    atomicAdd(&cnt[2], np);
     __syncthreads();
     if (tid == 0) {
         // the plane was chosen on estimated counts: keep it only if the
@@ -186,10 +275,18 @@ __global__ void __launch_bounds__(kBuildThreads) k_kd_choose(
         const double f = ((double)s - nd.mn[axis]) / ((double)nd.mx[axis] - nd.mn[axis]);
         const double sl = 2.0 * (f * da * db + f * da * dc + db * dc);
         const double sr = 2.0 * ((1.0 - f) * da * db + (1.0 - f) * da * dc + db * dc);
-        double c = cost.traversal + cost.intersection * (sl / sa * cnt[0] + sr / sa * cnt[1]);
-        if (cnt[0] == 0 || cnt[1] == 0) c *= cost.empty_bonus;
-        dec[blockIdx.x] = c < (double)cost.intersection * n ? LDec{axis, s, cnt[0], cnt[1]}
-                                                            : LDec{-1, 0.0f, 0, 0};
+        LDec best{-1, 0.0f, 0, 0, 0};
+        double bcost = (double)cost.intersection * n;
+        for (int side = 0; side < 2; side++) {  // the plane's own triangles left, then right
+            const int l2 = cnt[0] + (side == 0 ? cnt[2] : 0), r2 = cnt[1] + (side == 1 ? cnt[2] : 0);
+            double c = cost.traversal + cost.intersection * (sl / sa * l2 + sr / sa * r2);
+            if (l2 == 0 || r2 == 0) c *= cost.empty_bonus;
+            if (c < bcost) {
+                bcost = c;
+                best = LDec{axis, s, l2, r2, side == 0};
+            }
+        }
+        dec[blockIdx.x] = best;
     }
 }
 
@@ -334,7 +431,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_kd_write(
             const float l = fmaxf(lo[d.axis * ntri + t], nd.mn[d.axis]);
             const float h = fminf(hi[d.axis * ntri + t], nd.mx[d.axis]);
             if (l == h && l == d.split) {
-                gr = 1;
+                (d.planar_left ? gl : gr) = 1;
             } else {
                 gl = l < d.split;
                 gr = h > d.split;

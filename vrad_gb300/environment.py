@@ -213,7 +213,7 @@ class Environment:
                   "set_walk_tree_costs")
 
     def set_walk_tree_builder(self, mode):
-        """0 / False: host, 1 / True: GPU, -1: by scene size (the default)."""
+        """0 / False: host, 1 / True or -1 (the default): the context's GPU."""
         self._chk(self.lib.vrg_env_set_walk_tree_builder(self.h, int(mode)),
                   "set_walk_tree_builder")
 
