@@ -319,6 +319,33 @@ int vrg_env_bake(vrg_env *env, int32_t supersamples, uint64_t seed, int32_t max_
  * bounces run and the final energy delta. */
 int vrg_env_get_bake(vrg_env *env, float *luxel_rgb, float *patch_direct, float *patch_total,
                      int32_t *bounces, float *delta);
+
+/* ------------------------------------------------------------------ */
+/* Lightmap output: face extents and lightmap samples                  */
+/* (rad/world/face.go:14-90; cmd/tasks/finish/main.go:8-40 is a stub)  */
+/* ------------------------------------------------------------------ */
+
+/* CalcFaceExtents (rad/world/face.go:14-90) for one face: vertices (nverts
+ * x 3, winding order -- the surfedge walk of face.go:29-36 resolved by the
+ * caller: edge e >= 0 gives vertex edges[e][0], e < 0 gives edges[-e][1]),
+ * lightmap_vecs = the texinfo's LightmapVecsLuxelsPerWorldUnits (2 x 4).
+ * Writes LightmapTextureMinsInLuxels and LightmapTextureSizeInLuxels (the
+ * reference passes them by value and loses them, rad/start.go:110).
+ * *too_big (may be NULL) = 1 when a size exceeds 125 + 1, which the
+ * reference logs and carries on from.  Host only; needs no context. */
+int vrg_calc_face_extents(const float *vertices, int32_t nverts, const float *lightmap_vecs,
+                          int32_t *mins, int32_t *size, int32_t *too_big);
+/* Lightmap samples of the last bake (or relight) of this scene: per luxel,
+ * in the luxel order of vrg_env_gather_direct_light, the direct light plus
+ * the bounced light (TotalLight, common/types/patch.go:33) of the leaf patch
+ * holding the luxel centre, as one 4-byte shared-exponent sample
+ * {r, g, b, signed exponent x}, channel = byte * 2^x, x = max(e - 8, -128)
+ * for the largest channel m = f * 2^e (0.5 <= f < 1), byte = floor(channel
+ * * 2^-x); channels that are not > 0 store 0.  samples: 4 x num_luxels
+ * bytes; face_offset: nfaces + 1 byte offsets of each face's first sample
+ * (its lightofs in a lighting lump of one style).  Either may be NULL.
+ * Needs a bake of the current faces and patches (VRG_ERR_STATE otherwise). */
+int vrg_env_get_lightmap(vrg_env *env, uint8_t *samples, int64_t *face_offset);
 /* A batch of resident scenes baked together: the direct pass of every
  * scene in one persistent launch over a device work queue, then one
  * block-diagonal bounce loop (CUDA graph) with a per-scene stop. */

@@ -71,6 +71,11 @@ def lib():
         _lib.orc_make_patches.restype = C.c_int64
         _lib.orc_make_transfers.restype = C.c_int64
         _lib.orc_bounce_f64.restype = C.c_int
+        _lib.orc_encode_sample.restype = C.c_uint32
+        _lib.orc_encode_sample.argtypes = [C.c_float, C.c_float, C.c_float]
+        _lib.orc_calc_face_extents.restype = C.c_int
+        _lib.orc_calc_face_extents.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -308,3 +313,34 @@ def bounce_f64(row_ptr, col, w, refl, direct, base, max_bounces, tol):
                               _p(f32(refl)), _p(f32(direct)), _p(f32(base)), max_bounces,
                               C.c_double(tol), _p(total), _p(deltas))
     return total, it, deltas[:it]
+
+
+def encode_sample(r, g, b) -> int:
+    """Shared-exponent lightmap sample word of one light."""
+    return int(lib().orc_encode_sample(float(r), float(g), float(b)))
+
+
+def lightmap(lit, P, direct, total):
+    """Sample words (uint32 per luxel) of direct luxel light + bounced light of
+    the leaf patch at each luxel centre; P as make_patches returns it."""
+    off = lit.luxel_offset()
+    out = np.zeros(max(int(off[-1]), 1), np.uint32)
+    lib().orc_lightmap(_p(f32(lit.corner)), _p(f32(lit.u)), _p(f32(lit.v)), _p(f32(lit.normal)),
+                       _p(np.ascontiguousarray(lit.nu, np.int32)),
+                       _p(np.ascontiguousarray(lit.nv, np.int32)), _p(off),
+                       C.c_int32(lit.n_faces), _p(P["child1"]), _p(P["child2"]),
+                       _p(P["split_axis"]), _p(P["split_dist"]), _p(P["leaf_index"]),
+                       _p(P["face_root"]), _p(f32(direct)), _p(f32(total)), _p(out))
+    return out[: int(off[-1])]
+
+
+def calc_face_extents(vertices, lightmap_vecs):
+    """(mins, size, too_big) of CalcFaceExtents, or None for no vertices or
+    values beyond int32."""
+    v = f32(vertices).reshape(-1, 3)
+    vecs = f32(lightmap_vecs).reshape(2, 4)
+    mins, size, big = np.zeros(2, np.int32), np.zeros(2, np.int32), np.zeros(1, np.int32)
+    rc = lib().orc_calc_face_extents(_p(v), v.shape[0], _p(vecs), _p(mins), _p(size), _p(big))
+    if rc != 0:
+        return None
+    return (int(mins[0]), int(mins[1])), (int(size[0]), int(size[1])), bool(big[0])

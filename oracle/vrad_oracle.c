@@ -1610,3 +1610,100 @@ int orc_bounce_f64(int64_t nrows, const int64_t *row_ptr, const int32_t *col, co
     free(add);
     return b;
 }
+
+/* ---- lightmap samples (project semantics) ----
+ * The reference computes face extents and drops them (CalcFaceExtents takes
+ * its output arrays by value, rad/world/face.go:14, rad/start.go:110), its
+ * write-out is a stub (cmd/tasks/finish/main.go:8-40) and the sample encoder
+ * it names (compute/leafambient/lighting.go:67) is not in the project.
+ *
+ * Sample of one light: Ward's RGBE ("Real Pixels", Graphics Gems II) with a
+ * signed exponent byte.  A channel that is not > 0 counts as 0, +inf as
+ * FLT_MAX; m = the largest channel, 0 -> the all-zero sample; frexp gives
+ * m = f * 2^e with 0.5 <= f < 1; x = max(e - 8, -128);
+ * byte = floor(ldexp(c, -x)); the word is r | g << 8 | b << 16 | (x & 255) << 24. */
+static float sample_channel(float c) {
+    if (!(c > 0.0f)) return 0.0f;
+    return c > 3.4028234663852886e38f ? 3.4028234663852886e38f : c;
+}
+
+uint32_t orc_encode_sample(float r, float g, float b) {
+    float c[3] = {sample_channel(r), sample_channel(g), sample_channel(b)};
+    float m = c[0];
+    if (c[1] > m) m = c[1];
+    if (c[2] > m) m = c[2];
+    if (m == 0.0f) return 0u;
+    int e = 0;
+    (void)frexpf(m, &e);
+    int x = e - 8 < -128 ? -128 : e - 8;
+    uint32_t w = (uint32_t)(x & 255) << 24;
+    for (int a = 0; a < 3; a++) {
+        float s = floorf(ldexpf(c[a], -x));
+        w |= (uint32_t)(s > 255.0f ? 255.0f : s) << (8 * a);
+    }
+    return w;
+}
+
+/* Per luxel (face order, row-major nu x nv): light = direct[lux] +
+ * total[leaf], leaf = the face's patch tree descended at the luxel centre
+ * (the S == 1 sample point, centre + 0.125 N; coordinate >= dist ->
+ * child1), no bounced term when the face has no patches; then the sample. */
+void orc_lightmap(const float *corner, const float *u, const float *v, const float *nrm,
+                  const int32_t *nu, const int32_t *nv, const int64_t *luxel_offset,
+                  int32_t nfaces, const int32_t *child1, const int32_t *child2,
+                  const int32_t *split_axis, const float *split_dist, const int32_t *leaf_index,
+                  const int32_t *face_root, const float *direct, const float *total,
+                  uint32_t *out) {
+    for (int32_t f = 0; f < nfaces; f++)
+        for (int iv = 0; iv < nv[f]; iv++)
+            for (int iu = 0; iu < nu[f]; iu++) {
+                int64_t lux = luxel_offset[f] + (int64_t)iv * nu[f] + iu;
+                float light[3] = {direct[3 * lux], direct[3 * lux + 1], direct[3 * lux + 2]};
+                if (face_root[f] >= 0) {
+                    float p[3];
+                    luxel_sample(corner + 3 * f, u + 3 * f, v + 3 * f, nrm + 3 * f, nu[f], nv[f],
+                                 lux, iu, iv, 0, 1, 0, p);
+                    int32_t node = face_root[f];
+                    while (child1[node] >= 0)
+                        node = p[split_axis[node]] >= split_dist[node] ? child1[node] : child2[node];
+                    const float *t = total + 3 * (int64_t)leaf_index[node];
+                    for (int a = 0; a < 3; a++) light[a] = light[a] + t[a];
+                }
+                out[lux] = orc_encode_sample(light[0], light[1], light[2]);
+            }
+}
+
+/* CalcFaceExtents (rad/world/face.go:14-90) with its results returned: for
+ * each lightmap axis j, val = ((x*L[j][0] + y*L[j][1]) + z*L[j][2]) + L[j][3]
+ * over the face's vertices (float32, one rounding per operation), min/max
+ * seeded with +-1e24; mins = floor(min), size = ceil(max) - floor(min) (the
+ * subtraction in float32, then truncated to int32).  *too_big = 1 when a
+ * size exceeds 125 + 1 (MAX_LIGHTMAP_DIM_WITHOUT_BORDER, the same for
+ * displacements; common/constants/constants.go:22,27), which the reference
+ * logs and carries on from.  Returns 0, or -1 for no vertices or values that
+ * do not fit an int32. */
+int orc_calc_face_extents(const float *verts, int32_t nverts, const float *vecs,
+                          int32_t *mins_out, int32_t *size_out, int32_t *too_big) {
+    if (nverts < 1) return -1;
+    float mins[2] = {1e24f, 1e24f}, maxs[2] = {-1e24f, -1e24f};
+    for (int32_t i = 0; i < nverts; i++) {
+        const float *p = verts + 3 * i;
+        for (int j = 0; j < 2; j++) {
+            const float *L = vecs + 4 * j;
+            float val = ((p[0] * L[0] + p[1] * L[1]) + p[2] * L[2]) + L[3];
+            if (val < mins[j]) mins[j] = val;
+            if (val > maxs[j]) maxs[j] = val;
+        }
+    }
+    *too_big = 0;
+    for (int j = 0; j < 2; j++) {
+        float lo = (float)floor((double)mins[j]), hi = (float)ceil((double)maxs[j]);
+        float sz = hi - lo;
+        if (!(lo >= -2147483648.0f && lo < 2147483648.0f && sz >= -2147483648.0f && sz < 2147483648.0f))
+            return -1;
+        mins_out[j] = (int32_t)lo;
+        size_out[j] = (int32_t)sz;
+        if (size_out[j] > 125 + 1) *too_big = 1;
+    }
+    return 0;
+}

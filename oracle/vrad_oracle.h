@@ -19,6 +19,7 @@
  *   vmath/quadratic/solver.go:4-63             inverse quadratic solve
  *   rad/patches/subdivide.go:166-411           patch subdivision
  *   common/types/patch.go, transfer.go         patch / transfer layout
+ *   rad/world/face.go:14-90                    face lightmap extents
  * Gather, transfer building and the bounce loop are absent from the
  * reference; their semantics are the project's own and are written out in
  * the comments of vrad_oracle.c beside each function.
@@ -175,6 +176,21 @@ int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t 
 int orc_bounce_f64(int64_t nrows, const int64_t *row_ptr, const int32_t *col, const float *w,
                    const float *refl, const float *direct, const float *base, int max_bounces,
                    double tol, double *out_total, double *out_deltas);
+
+/* ---- lightmap samples ---- */
+/* Shared-exponent sample (r | g << 8 | b << 16 | exponent << 24) of one light. */
+uint32_t orc_encode_sample(float r, float g, float b);
+/* Samples of every luxel: direct light + bounced light of the leaf patch at
+ * the luxel centre.  direct: 3 floats per luxel; total: 3 floats per leaf. */
+void orc_lightmap(const float *corner, const float *u, const float *v, const float *nrm,
+                  const int32_t *nu, const int32_t *nv, const int64_t *luxel_offset,
+                  int32_t nfaces, const int32_t *child1, const int32_t *child2,
+                  const int32_t *split_axis, const float *split_dist, const int32_t *leaf_index,
+                  const int32_t *face_root, const float *direct, const float *total,
+                  uint32_t *out);
+/* CalcFaceExtents: vecs = LightmapVecsLuxelsPerWorldUnits (2 x 4 floats). */
+int orc_calc_face_extents(const float *verts, int32_t nverts, const float *vecs,
+                          int32_t *mins_out, int32_t *size_out, int32_t *too_big);
 
 #ifdef __cplusplus
 }

@@ -82,6 +82,8 @@ SIGNATURES = {
     "vrg_env_bounce_light_noalloc": (C.c_int, [P, I32, F, P, P, P]),
     "vrg_env_bake": (C.c_int, [P, I32, U64, I32, F, P]),
     "vrg_env_get_bake": (C.c_int, [P, P, P, P, P, P]),
+    "vrg_calc_face_extents": (C.c_int, [P, I32, P, P, P, P]),
+    "vrg_env_get_lightmap": (C.c_int, [P, P, P]),
     "vrg_batch_create": (C.c_int, [P, P]),
     "vrg_batch_destroy": (None, [P]),
     "vrg_batch_add": (C.c_int, [P, P]),

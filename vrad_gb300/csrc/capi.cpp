@@ -525,6 +525,47 @@ int vrg_env_set_lights(vrg_env *env, const vrg_light *lights, int32_t n) {
     return sync(env->ctx);
 }
 
+/* ---------------- face lightmap extents ---------------- */
+
+// CalcFaceExtents (rad/world/face.go:14-90), with the two results written
+// out (the reference takes them by value and loses them, rad/start.go:110).
+// Each vertex is projected onto both lightmap axes in float32, one rounding
+// per operation: ((x*L0 + y*L1) + z*L2) + L3; the running bounds start at
+// +-1e24; mins = floor(min) and size = ceil(max) - floor(min), the
+// subtraction in float32.  A size above the lightmap limit + 1 (125,
+// common/constants/constants.go:22,27, for brush and displacement faces
+// alike) is reported in *too_big, the case the reference logs and goes on.
+int vrg_calc_face_extents(const float *vertices, int32_t nverts, const float *lightmap_vecs,
+                          int32_t *mins, int32_t *size, int32_t *too_big) {
+    if (!vertices || nverts < 1 || !lightmap_vecs || !mins || !size) return VRG_ERR_INVALID;
+    float lo[2] = {1e24f, 1e24f}, hi[2] = {-1e24f, -1e24f};
+    for (int32_t i = 0; i < nverts; i++) {
+        const float *p = vertices + 3 * i;
+        for (int j = 0; j < 2; j++) {
+            const float *L = lightmap_vecs + 4 * j;
+            const float val = ((p[0] * L[0] + p[1] * L[1]) + p[2] * L[2]) + L[3];
+            lo[j] = val < lo[j] ? val : lo[j];
+            hi[j] = val > hi[j] ? val : hi[j];
+        }
+    }
+    int32_t m[2], s[2], big = 0;
+    for (int j = 0; j < 2; j++) {
+        const float fl = (float)std::floor((double)lo[j]), ce = (float)std::ceil((double)hi[j]);
+        const float extent = ce - fl;
+        if (!(fl >= -2147483648.0f && fl < 2147483648.0f && extent >= -2147483648.0f && extent < 2147483648.0f))
+            return VRG_ERR_INVALID;  // non-finite or beyond int32
+        m[j] = (int32_t)fl;
+        s[j] = (int32_t)extent;
+        big |= s[j] > kMaxLightmapDim + 1 ? 1 : 0;
+    }
+    mins[0] = m[0];
+    mins[1] = m[1];
+    size[0] = s[0];
+    size[1] = s[1];
+    if (too_big) *too_big = big;
+    return VRG_OK;
+}
+
 /* ---------------- faces and the direct-light gather ---------------- */
 
 int vrg_env_set_faces(vrg_env *env, int32_t nfaces, const float *corner, const float *u, const float *v,
@@ -578,6 +619,7 @@ int vrg_env_set_faces(vrg_env *env, int32_t nfaces, const float *corner, const f
     TRY(upload(ctx, env->d_luxel_offset, env->luxel_offset.data(), env->luxel_offset.size() * 8));
     TRY(upload(ctx, env->d_tri_face, env->tri_face.data(), std::max<size_t>(1, env->tri_face.size()) * 4));
     env->have_patches = env->have_transfers = env->have_patch_direct = false;
+    env->have_bake = false;  // the last bake's buffers were sized for the old faces
     return sync(ctx);
 }
 
@@ -695,6 +737,7 @@ int vrg_env_make_patches(vrg_env *env, float max_chop, float min_chop, int64_t *
     }
     env->have_patches = true;
     env->have_transfers = env->have_patch_direct = false;
+    env->have_bake = false;  // the last bake's bounced light belongs to the old leaves
     if (num_patches) *num_patches = (int64_t)n;
     if (num_leaves) *num_leaves = (int64_t)nl;
     return sync(ctx);

@@ -20,6 +20,9 @@ constexpr int kCostOfTraversal = 75;
 constexpr int kCostOfIntersection = 167;
 constexpr int kMaxTreeDepth = 21;
 constexpr uint32_t kLeaf = 3;  // KDNODE_STATE_LEAF (raytracer/cache/optimisedkdnode.go:6)
+// MAX_LIGHTMAP_DIM_WITHOUT_BORDER = MAX_DISP_LIGHTMAP_DIM_WITHOUT_BORDER
+// (common/constants/constants.go:22,27)
+constexpr int32_t kMaxLightmapDim = 125;
 
 struct Error {
     int code;

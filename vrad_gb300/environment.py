@@ -134,6 +134,19 @@ def make_light(type_, origin, intensity, normal=(0.0, 0.0, -1.0), **keys) -> Lig
     return li
 
 
+def calc_face_extents(vertices, lightmap_vecs):
+    """CalcFaceExtents (rad/world/face.go:14-90): LightmapTextureMinsInLuxels,
+    LightmapTextureSizeInLuxels and whether the face is too big for a lightmap,
+    from the face's vertices (winding order) and LightmapVecsLuxelsPerWorldUnits."""
+    lib = _lib.load()
+    v = _f32(vertices, (-1, 3))
+    vecs = _f32(lightmap_vecs, (2, 4))
+    mins, size, big = np.zeros(2, np.int32), np.zeros(2, np.int32), np.zeros(1, np.int32)
+    check(lib.vrg_calc_face_extents(_p(v), v.shape[0], _p(vecs), _p(mins), _p(size), _p(big)),
+          None, "calc_face_extents")
+    return (int(mins[0]), int(mins[1])), (int(size[0]), int(size[1])), bool(big[0])
+
+
 def light_array(lights) -> "C.Array":
     arr = (Light * max(len(lights), 1))()
     for i, li in enumerate(lights):
@@ -406,6 +419,16 @@ class Environment:
                                             C.byref(d)), "get_bake")
         return dict(luxels=lux, patch_direct=direct, patch_total=total, bounces=b.value,
                     delta=d.value)
+
+    def get_lightmap(self):
+        """Lightmap samples of the last bake: (num_luxels, 4) uint8 shared-exponent
+        samples (r, g, b, signed exponent) and the nfaces + 1 byte offsets of each
+        face's first sample."""
+        samples = np.empty((self.num_luxels(), 4), np.uint8)
+        nf = len(self._faces["nu"]) if hasattr(self, "_faces") else 0
+        offsets = np.empty(nf + 1, np.int64)
+        self._chk(self.lib.vrg_env_get_lightmap(self.h, _p(samples), _p(offsets)), "get_lightmap")
+        return samples, offsets
 
     def bounce_light(self, n_leaves, max_bounces=100, rel_tol=1e-3):
         total = np.empty((n_leaves, 3), np.float32)
