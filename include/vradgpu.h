@@ -47,6 +47,15 @@ extern "C" {
 #define VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_COLORS 2
 #define VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_MATERIALS 4
 
+/* BSP contents and surface flags the brush ingest reads (Source's bspflags
+ * values, which galaco/bsp's flags package carries):
+ * MASK_OPAQUE = CONTENTS_SOLID | CONTENTS_MOVEABLE | CONTENTS_OPAQUE. */
+#define VRG_CONTENTS_SOLID 0x1
+#define VRG_CONTENTS_OPAQUE 0x80
+#define VRG_CONTENTS_MOVEABLE 0x4000
+#define VRG_MASK_OPAQUE (VRG_CONTENTS_SOLID | VRG_CONTENTS_MOVEABLE | VRG_CONTENTS_OPAQUE)
+#define VRG_SURF_SKY 0x4
+
 /* Source's emittype order, as galaco/bsp worldlight EMIT_* uses it. */
 #define VRG_EMIT_SURFACE 0
 #define VRG_EMIT_POINT 1
@@ -102,7 +111,8 @@ int vrg_ctx_set_timing(vrg_ctx *ctx, int enable);
  * reset; names: "trace_mask", "trace_closest", "trace_lines",
  * "direct_luxels", "direct_points", "transfer_rows", "transfer_gather",
  * "bounce_init", "bounce_spmv", "bounce_reduce", "batch_gather",
- * "batch_bounce_init", "batch_spmv", "batch_reduce", "relight_gather". */
+ * "batch_bounce_init", "batch_spmv", "batch_reduce", "relight_gather",
+ * "lightmap". */
 int vrg_ctx_kernel_stats(vrg_ctx *ctx, const char *name, double *total_ms, int64_t *launches);
 int vrg_ctx_reset_stats(vrg_ctx *ctx);
 /* Kernels launched by this context since creation (all names). */
@@ -142,6 +152,75 @@ int vrg_env_add_axis_aligned_rectangular_solid(vrg_env *env, int32_t id, const f
 /* Bulk AddTriangle for n triangles (xyz: 9 floats each), the loop of
  * cmd/tasks/loadbsp/main.go:276,338. */
 int vrg_env_add_triangles(vrg_env *env, const float *xyz, const int32_t *ids, int64_t n);
+
+/* The lumps of a compiled map that addBrushesForRayTrace reads
+ * (cmd/tasks/loadbsp/main.go:284-340), as arrays the caller has parsed
+ * (lump records reduced to the fields used; counts are record counts).
+ * planes: num_planes x {normal xyz, dist}, in the BSP's pairs (p ^ 1 is p
+ * facing the other way); node_children: num_nodes x {child0, child1}
+ * (negative = -1 - leaf); leaf_brush_ranges: num_leafs x {firstleafbrush,
+ * numleafbrushes}; leaf_brushes: brush indices; brushes: num_brushes x
+ * {firstside, numsides, contents}; brush_sides: num_brush_sides x {planenum,
+ * texinfo (-1: none), dispinfo, bevel}; texinfo_flags: num_texinfo surface
+ * flags; vertexes: num_vertexes x xyz; edges: num_edges x {v0, v1};
+ * surf_edges: signed edge indices; faces: num_faces x {firstedge, numedges,
+ * texinfo}.  headnode, first_face and num_model_faces describe model 0 (the
+ * world). */
+typedef struct vrg_bsp_world {
+    const float *planes;
+    int32_t num_planes;
+    const int32_t *node_children;
+    int32_t num_nodes;
+    const int32_t *leaf_brush_ranges;
+    int32_t num_leafs;
+    const int32_t *leaf_brushes;
+    int32_t num_leaf_brushes;
+    const int32_t *brushes;
+    int32_t num_brushes;
+    const int32_t *brush_sides;
+    int32_t num_brush_sides;
+    const int32_t *texinfo_flags;
+    int32_t num_texinfo;
+    const float *vertexes;
+    int32_t num_vertexes;
+    const int32_t *edges;
+    int32_t num_edges;
+    const int32_t *surf_edges;
+    int32_t num_surf_edges;
+    const int32_t *faces;
+    int32_t num_faces;
+    int32_t headnode;
+    int32_t first_face;
+    int32_t num_model_faces;
+} vrg_bsp_world;
+/* addBrushesForRayTrace (cmd/tasks/loadbsp/main.go:284-340) and
+ * addBrushToRaytraceEnvironment (:241-282): every opaque brush (contents &
+ * VRG_MASK_OPAQUE) of the world, in GetBrushRecursive order (brush.go:7-36),
+ * adds each side that is neither sky nor a displacement as the fan of its
+ * winding -- BaseWindingForPlane chopped by every other non-bevel side's
+ * flipped plane (planenum ^ 1) -- with id VRG_TRACE_ID_OPAQUE; then every
+ * sky face of the world adds the fan of its vertices with id
+ * VRG_TRACE_ID_SKY.  Colour (1, 0, 0) as the reference's fullCoverage.  The
+ * reference adds only the sky sides of brushes (an inverted test at
+ * main.go:255); sky sides are skipped here.  Every index is checked before a
+ * triangle is added (VRG_ERR_INVALID); the counts of brush and sky
+ * triangles added may be returned (NULL to skip). */
+int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *brush_triangles,
+                          int64_t *sky_triangles);
+/* BaseWindingForPlane (vmath/polygon/winding.go:26-83): the quad
+ * (4 x xyz) of half-side 65536 on the plane, around normal * dist. */
+int vrg_base_winding_for_plane(const float *normal, float dist, float *out12);
+/* ChopWindingInPlace (winding.go:85-170): the part of the n-point winding
+ * in front of the plane (points with normal . p - dist >= -epsilon kept,
+ * crossing edges split); *out_n = 0 when nothing is in front.  out holds up
+ * to n + 4 points; more than 64 points give VRG_ERR_UNSUPPORTED. */
+int vrg_chop_winding(const float *points, int32_t n, const float *normal, float dist, float epsilon,
+                     float *out, int32_t *out_n);
+/* The vertices (9 floats) and ids of triangles [first, first + n) in the
+ * order they were added (OptimisedTriangle.Vertex, raytracer/cache/
+ * optimisedtriangle.go:22-28, reading x, y, z). */
+int vrg_env_get_triangle_vertices(const vrg_env *env, int64_t first, int64_t n, float *xyz,
+                                  int32_t *ids);
 /* SetupAccelerationStructure (environment.go:119-138): builds on the host
  * and uploads the tree the device walks (the walk tree: the reference's node
  * format, SAH over every candidate plane) with the intersection records;

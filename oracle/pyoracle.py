@@ -344,3 +344,53 @@ def calc_face_extents(vertices, lightmap_vecs):
     if rc != 0:
         return None
     return (int(mins[0]), int(mins[1])), (int(size[0]), int(size[1])), bool(big[0])
+
+
+def base_winding(normal, dist):
+    out = np.zeros((4, 3), np.float32)
+    lib().orc_base_winding(_p(f32(normal)), C.c_float(dist), _p(out))
+    return out
+
+
+def chop_winding(points, normal, dist, eps=0.0):
+    """The part of the winding in front of the plane, or None past 64 points."""
+    pts = f32(points).reshape(-1, 3)
+    w = np.zeros((68, 3), np.float32)
+    w[: len(pts)] = pts
+    n = lib().orc_chop_winding(_p(w), C.c_int(len(pts)), _p(f32(normal)), C.c_float(dist),
+                               C.c_float(eps))
+    return None if n < 0 else w[:n].copy()
+
+
+def bsp_world_triangles(lumps, headnode=0, first_face=0, num_model_faces=None):
+    """(xyz (n, 9), ids, brush triangle count) of the world's brushes and sky faces."""
+    def arr(name, dt, per):
+        return np.ascontiguousarray(lumps.get(name, np.zeros((0, per))), dtype=dt).reshape(-1, per)
+
+    planes = arr("planes", np.float32, 4)
+    children = arr("node_children", np.int32, 2)
+    ranges = arr("leaf_brush_ranges", np.int32, 2)
+    lb = arr("leaf_brushes", np.int32, 1)
+    brushes = arr("brushes", np.int32, 3)
+    sides = arr("brush_sides", np.int32, 4)
+    tflags = arr("texinfo_flags", np.int32, 1)
+    verts = arr("vertexes", np.float32, 3)
+    edges = arr("edges", np.int32, 2)
+    se = arr("surf_edges", np.int32, 1)
+    faces = arr("faces", np.int32, 3)
+    nmf = len(faces) - first_face if num_model_faces is None else num_model_faces
+    cap = 64 * len(sides) + 64 * len(faces) + 1
+    xyz = np.zeros((cap, 9), np.float32)
+    ids = np.zeros(cap, np.int32)
+    nb = C.c_int64()
+    L = lib()
+    L.orc_bsp_world_triangles.restype = C.c_int64
+    n = L.orc_bsp_world_triangles(_p(planes), _p(children), C.c_int32(len(children)), _p(ranges),
+                                  C.c_int32(len(ranges)), _p(lb), _p(brushes),
+                                  C.c_int32(len(brushes)), _p(sides), _p(tflags), _p(verts),
+                                  _p(edges), _p(se), _p(faces), C.c_int32(headnode),
+                                  C.c_int32(first_face), C.c_int32(nmf), _p(xyz), _p(ids),
+                                  C.c_int64(cap), C.byref(nb))
+    if n < 0:
+        return None
+    return xyz[:n].copy(), ids[:n].copy(), nb.value

@@ -1707,3 +1707,173 @@ int orc_calc_face_extents(const float *verts, int32_t nverts, const float *vecs,
     }
     return 0;
 }
+
+/* ---- brush ingest (fixed mode) ----
+ * addBrushesForRayTrace / addBrushToRaytraceEnvironment
+ * (cmd/tasks/loadbsp/main.go:241-340), BaseWindingForPlane and
+ * ChopWindingInPlace (vmath/polygon/winding.go:26-170), with the defects the
+ * fixed mode repairs: sky sides are skipped (the reference keeps only them,
+ * main.go:255); the major axis reads normal[i] and axes 0 and 1 share the
+ * up vector (0,0,1) (winding.go:36,45-51); the fourth point is written
+ * (winding.go:77-78); the wrap-around side/distance entry is set and the
+ * split loop advances j (winding.go:100-114,148).  No literal mode: the Go
+ * as written never leaves the split loop. */
+#define ORC_WPTS 68
+
+static float dot3f(const float *a, const float *b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+void orc_base_winding(const float *n, float dist, float *out12) {
+    int x = -1;
+    float mx = -1.0f;
+    for (int i = 0; i < 3; i++) {
+        float v = fabsf(n[i]);
+        if (v > mx) { x = i; mx = v; }
+    }
+    float up[3] = {0.0f, 0.0f, 0.0f};
+    if (x == 0 || x == 1) up[2] = 1.0f;
+    else up[0] = 1.0f;
+    float v = dot3f(up, n);
+    for (int a = 0; a < 3; a++) up[a] = up[a] + (-v) * n[a];
+    float il = 1.0f / sqrtf(dot3f(up, up));
+    for (int a = 0; a < 3; a++) up[a] = up[a] * il;
+    float org[3], right[3];
+    for (int a = 0; a < 3; a++) org[a] = n[a] * dist;
+    right[0] = up[1] * n[2] - up[2] * n[1];
+    right[1] = up[2] * n[0] - up[0] * n[2];
+    right[2] = up[0] * n[1] - up[1] * n[0];
+    for (int a = 0; a < 3; a++) {
+        up[a] = up[a] * 65536.0f;
+        right[a] = right[a] * 65536.0f;
+    }
+    for (int a = 0; a < 3; a++) {
+        out12[0 + a] = (org[a] - right[a]) + up[a];
+        out12[3 + a] = (org[a] + right[a]) + up[a];
+        out12[6 + a] = (org[a] + right[a]) - up[a];
+        out12[9 + a] = (org[a] - right[a]) - up[a];
+    }
+}
+
+/* In-place chop of w (n points, room for ORC_WPTS); returns the new count
+ * (0: nothing in front) or -1 past 64 points. */
+int orc_chop_winding(float *w, int n, const float *nrm, float dist, float eps) {
+    float dists[ORC_WPTS + 1], tmp[3 * ORC_WPTS];
+    int sides[ORC_WPTS + 1], counts[3] = {0, 0, 0};
+    if (n <= 0) return 0;
+    for (int i = 0; i < n; i++) {
+        dists[i] = dot3f(w + 3 * i, nrm) - dist;
+        sides[i] = dists[i] > eps ? 0 : (dists[i] < -eps ? 1 : 2);
+        counts[sides[i]]++;
+    }
+    sides[n] = sides[0];
+    dists[n] = dists[0];
+    if (counts[0] == 0) return 0;
+    if (counts[1] == 0) return n;
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+        const float *p1 = w + 3 * i;
+        if (sides[i] == 2) {
+            if (m >= ORC_WPTS) return -1;
+            memcpy(tmp + 3 * m++, p1, 12);
+            continue;
+        }
+        if (sides[i] == 0) {
+            if (m >= ORC_WPTS) return -1;
+            memcpy(tmp + 3 * m++, p1, 12);
+        }
+        if (sides[i + 1] == 2 || sides[i + 1] == sides[i]) continue;
+        const float *p2 = w + 3 * ((i + 1) % n);
+        float t = dists[i] / (dists[i] - dists[i + 1]);
+        if (m >= ORC_WPTS) return -1;
+        for (int j = 0; j < 3; j++) {
+            if (nrm[j] == 1.0f) tmp[3 * m + j] = dist;
+            else if (nrm[j] == -1.0f) tmp[3 * m + j] = -dist;
+            else tmp[3 * m + j] = p1[j] + t * (p2[j] - p1[j]);
+        }
+        m++;
+    }
+    if (m > 64) return -1;
+    memcpy(w, tmp, 12 * (size_t)m);
+    return m;
+}
+
+static void brushes_recursive(int32_t node, const int32_t *children, const int32_t *leaf_ranges,
+                              const int32_t *leaf_brushes, int32_t *list, int32_t *count) {
+    if (node < 0) {
+        int32_t leaf = -1 - node;
+        for (int32_t i = 0; i < leaf_ranges[2 * leaf + 1]; i++) {
+            int32_t b = leaf_brushes[leaf_ranges[2 * leaf] + i], found = 0;
+            for (int32_t k = 0; k < *count; k++)
+                if (list[k] == b) { found = 1; break; }
+            if (!found) list[(*count)++] = b;
+        }
+        return;
+    }
+    brushes_recursive(children[2 * node], children, leaf_ranges, leaf_brushes, list, count);
+    brushes_recursive(children[2 * node + 1], children, leaf_ranges, leaf_brushes, list, count);
+}
+
+/* Triangles of the world (model 0): opaque brushes then sky faces, in the
+ * reference's order; ids ORC_TRACE_ID_OPAQUE / ORC_TRACE_ID_SKY.  Inputs are
+ * assumed valid (the tests build them).  Returns the triangle count, or -1
+ * when cap is too small or a winding passes 64 points; *n_brush = brush
+ * triangles. */
+int64_t orc_bsp_world_triangles(const float *planes, const int32_t *node_children, int32_t num_nodes,
+                                const int32_t *leaf_ranges, int32_t num_leafs,
+                                const int32_t *leaf_brushes, const int32_t *brushes,
+                                int32_t num_brushes, const int32_t *brush_sides,
+                                const int32_t *texinfo_flags, const float *vertexes,
+                                const int32_t *edges, const int32_t *surf_edges,
+                                const int32_t *faces, int32_t headnode, int32_t first_face,
+                                int32_t num_model_faces, float *xyz, int32_t *ids, int64_t cap,
+                                int64_t *n_brush) {
+    int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)(num_brushes > 0 ? num_brushes : 1));
+    int32_t count = 0;
+    int64_t nt = 0;
+    if (num_nodes > 0 || num_leafs > 0)
+        brushes_recursive(headnode, node_children, leaf_ranges, leaf_brushes, list, &count);
+    float w[3 * ORC_WPTS];
+    for (int32_t k = 0; k < count; k++) {
+        const int32_t *b = brushes + 3 * list[k];
+        if ((b[2] & (0x1 | 0x4000 | 0x80)) == 0) continue;
+        for (int32_t i = 0; i < b[1]; i++) {
+            const int32_t *side = brush_sides + 4 * (b[0] + i);
+            int32_t tf = side[1] >= 0 ? texinfo_flags[side[1]] : 0;
+            if ((tf & 0x4) != 0 || side[2] != 0) continue;
+            orc_base_winding(planes + 4 * side[0], planes[4 * side[0] + 3], w);
+            int n = 4;
+            for (int32_t j = 0; j < b[1] && n > 0; j++) {
+                if (j == i) continue;
+                const int32_t *o = brush_sides + 4 * (b[0] + j);
+                if (o[3] != 0) continue;
+                const float *op = planes + 4 * (o[0] ^ 1);
+                n = orc_chop_winding(w, n, op, op[3], 0.0f);
+                if (n < 0) { free(list); return -1; }
+            }
+            for (int j = 2; j < n; j++) {
+                if (nt >= cap) { free(list); return -1; }
+                memcpy(xyz + 9 * nt, w, 12);
+                memcpy(xyz + 9 * nt + 3, w + 3 * (j - 1), 12);
+                memcpy(xyz + 9 * nt + 6, w + 3 * j, 12);
+                ids[nt++] = ORC_TRACE_ID_OPAQUE;
+            }
+        }
+    }
+    free(list);
+    *n_brush = nt;
+    for (int32_t k = 0; k < num_model_faces; k++) {
+        const int32_t *f = faces + 3 * (first_face + k);
+        int32_t tf = f[2] >= 0 ? texinfo_flags[f[2]] : 0;
+        if ((tf & 0x4) == 0) continue;
+        for (int32_t j = 2; j < f[1]; j++) {
+            int32_t vv[3] = {0, j - 1, j};
+            if (nt >= cap) return -1;
+            for (int c = 0; c < 3; c++) {
+                int32_t e = surf_edges[f[0] + vv[c]];
+                int32_t v = e < 0 ? edges[2 * (-e) + 1] : edges[2 * e];
+                memcpy(xyz + 9 * nt + 3 * c, vertexes + 3 * v, 12);
+            }
+            ids[nt++] = ORC_TRACE_ID_SKY;
+        }
+    }
+    return nt;
+}

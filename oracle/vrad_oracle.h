@@ -20,6 +20,8 @@
  *   rad/patches/subdivide.go:166-411           patch subdivision
  *   common/types/patch.go, transfer.go         patch / transfer layout
  *   rad/world/face.go:14-90                    face lightmap extents
+ *   cmd/tasks/loadbsp/main.go:241-340          brushes and sky faces -> triangles
+ *   vmath/polygon/winding.go:26-170            base winding, winding chop
  * Gather, transfer building and the bounce loop are absent from the
  * reference; their semantics are the project's own and are written out in
  * the comments of vrad_oracle.c beside each function.
@@ -191,6 +193,21 @@ void orc_lightmap(const float *corner, const float *u, const float *v, const flo
 /* CalcFaceExtents: vecs = LightmapVecsLuxelsPerWorldUnits (2 x 4 floats). */
 int orc_calc_face_extents(const float *verts, int32_t nverts, const float *vecs,
                           int32_t *mins_out, int32_t *size_out, int32_t *too_big);
+
+/* ---- brush ingest (fixed mode) ---- */
+void orc_base_winding(const float *n, float dist, float *out12);
+/* w has room for 68 points; returns the new point count, 0 = nothing in
+ * front, -1 = past 64 points. */
+int orc_chop_winding(float *w, int n, const float *nrm, float dist, float eps);
+int64_t orc_bsp_world_triangles(const float *planes, const int32_t *node_children, int32_t num_nodes,
+                                const int32_t *leaf_ranges, int32_t num_leafs,
+                                const int32_t *leaf_brushes, const int32_t *brushes,
+                                int32_t num_brushes, const int32_t *brush_sides,
+                                const int32_t *texinfo_flags, const float *vertexes,
+                                const int32_t *edges, const int32_t *surf_edges,
+                                const int32_t *faces, int32_t headnode, int32_t first_face,
+                                int32_t num_model_faces, float *xyz, int32_t *ids, int64_t cap,
+                                int64_t *n_brush);
 
 #ifdef __cplusplus
 }

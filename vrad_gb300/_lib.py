@@ -84,6 +84,10 @@ SIGNATURES = {
     "vrg_env_get_bake": (C.c_int, [P, P, P, P, P, P]),
     "vrg_calc_face_extents": (C.c_int, [P, I32, P, P, P, P]),
     "vrg_env_get_lightmap": (C.c_int, [P, P, P]),
+    "vrg_env_add_bsp_world": (C.c_int, [P, P, P, P]),
+    "vrg_base_winding_for_plane": (C.c_int, [P, F, P]),
+    "vrg_chop_winding": (C.c_int, [P, I32, P, F, F, P, P]),
+    "vrg_env_get_triangle_vertices": (C.c_int, [P, I64, I64, P, P]),
     "vrg_batch_create": (C.c_int, [P, P]),
     "vrg_batch_destroy": (None, [P]),
     "vrg_batch_add": (C.c_int, [P, P]),

@@ -134,6 +134,73 @@ def make_light(type_, origin, intensity, normal=(0.0, 0.0, -1.0), **keys) -> Lig
     return li
 
 
+class BspWorld(C.Structure):
+    """vrg_bsp_world: the lump arrays addBrushesForRayTrace reads."""
+
+    _fields_ = [("planes", C.c_void_p), ("num_planes", C.c_int32),
+                ("node_children", C.c_void_p), ("num_nodes", C.c_int32),
+                ("leaf_brush_ranges", C.c_void_p), ("num_leafs", C.c_int32),
+                ("leaf_brushes", C.c_void_p), ("num_leaf_brushes", C.c_int32),
+                ("brushes", C.c_void_p), ("num_brushes", C.c_int32),
+                ("brush_sides", C.c_void_p), ("num_brush_sides", C.c_int32),
+                ("texinfo_flags", C.c_void_p), ("num_texinfo", C.c_int32),
+                ("vertexes", C.c_void_p), ("num_vertexes", C.c_int32),
+                ("edges", C.c_void_p), ("num_edges", C.c_int32),
+                ("surf_edges", C.c_void_p), ("num_surf_edges", C.c_int32),
+                ("faces", C.c_void_p), ("num_faces", C.c_int32),
+                ("headnode", C.c_int32), ("first_face", C.c_int32),
+                ("num_model_faces", C.c_int32)]
+
+    # (field, dtype, values per record)
+    LUMPS = [("planes", np.float32, 4), ("node_children", np.int32, 2),
+             ("leaf_brush_ranges", np.int32, 2), ("leaf_brushes", np.int32, 1),
+             ("brushes", np.int32, 3), ("brush_sides", np.int32, 4),
+             ("texinfo_flags", np.int32, 1), ("vertexes", np.float32, 3), ("edges", np.int32, 2),
+             ("surf_edges", np.int32, 1), ("faces", np.int32, 3)]
+    COUNTS = {"planes": "num_planes", "node_children": "num_nodes",
+              "leaf_brush_ranges": "num_leafs", "leaf_brushes": "num_leaf_brushes",
+              "brushes": "num_brushes", "brush_sides": "num_brush_sides",
+              "texinfo_flags": "num_texinfo", "vertexes": "num_vertexes", "edges": "num_edges",
+              "surf_edges": "num_surf_edges", "faces": "num_faces"}
+
+    @classmethod
+    def from_arrays(cls, lumps: dict, headnode: int = 0, first_face: int = 0,
+                    num_model_faces: int | None = None):
+        """lumps maps each field name to an array of records; returns the
+        structure and the contiguous arrays it points into (keep them alive)."""
+        w = cls()
+        keep = []
+        for name, dt, per in cls.LUMPS:
+            a = np.ascontiguousarray(lumps.get(name, np.zeros((0, per))), dtype=dt).reshape(-1, per)
+            keep.append(a)
+            setattr(w, name, a.ctypes.data if a.size else None)
+            setattr(w, cls.COUNTS[name], a.shape[0])
+        w.headnode = headnode
+        w.first_face = first_face
+        w.num_model_faces = w.num_faces - first_face if num_model_faces is None else num_model_faces
+        return w, keep
+
+
+def base_winding_for_plane(normal, dist):
+    """BaseWindingForPlane (vmath/polygon/winding.go:26-83): 4 x 3 float32."""
+    lib = _lib.load()
+    out = np.zeros((4, 3), np.float32)
+    check(lib.vrg_base_winding_for_plane(_p(_f32(normal, (3,))), float(dist), _p(out)), None,
+          "base_winding_for_plane")
+    return out
+
+
+def chop_winding(points, normal, dist, epsilon=0.0):
+    """ChopWindingInPlace (winding.go:85-170): the part in front of the plane."""
+    lib = _lib.load()
+    pts = _f32(points, (-1, 3))
+    out = np.zeros((pts.shape[0] + 4, 3), np.float32)
+    n = np.zeros(1, np.int32)
+    check(lib.vrg_chop_winding(_p(pts), pts.shape[0], _p(_f32(normal, (3,))), float(dist),
+                               float(epsilon), _p(out), _p(n)), None, "chop_winding")
+    return out[: n[0]]
+
+
 def calc_face_extents(vertices, lightmap_vecs):
     """CalcFaceExtents (rad/world/face.go:14-90): LightmapTextureMinsInLuxels,
     LightmapTextureSizeInLuxels and whether the face is too big for a lightmap,
@@ -205,6 +272,26 @@ class Environment:
     def SetupAccelerationStructure(self):
         self._chk(self.lib.vrg_env_setup_acceleration_structure(self.h),
                   "SetupAccelerationStructure")
+
+    def add_bsp_world(self, lumps: dict, headnode: int = 0, first_face: int = 0,
+                      num_model_faces: int | None = None):
+        """addBrushesForRayTrace (cmd/tasks/loadbsp/main.go:284-340): the world's
+        opaque brushes and sky faces as triangles; returns (brush, sky) counts."""
+        w, keep = BspWorld.from_arrays(lumps, headnode, first_face, num_model_faces)
+        nb, ns = C.c_int64(), C.c_int64()
+        self._chk(self.lib.vrg_env_add_bsp_world(self.h, C.byref(w), C.byref(nb), C.byref(ns)),
+                  "add_bsp_world")
+        del keep
+        return nb.value, ns.value
+
+    def get_triangle_vertices(self, first: int = 0, n: int | None = None):
+        """(n, 9) vertices and (n,) ids of the triangles added so far."""
+        n = self.num_triangles() - first if n is None else n
+        xyz = np.zeros((n, 9), np.float32)
+        ids = np.zeros(n, np.int32)
+        self._chk(self.lib.vrg_env_get_triangle_vertices(self.h, first, n, _p(xyz), _p(ids)),
+                  "get_triangle_vertices")
+        return xyz, ids
 
     def num_triangles(self) -> int:
         return int(self.lib.vrg_env_num_triangles(self.h))
