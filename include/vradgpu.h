@@ -154,7 +154,7 @@ int vrg_env_add_axis_aligned_rectangular_solid(vrg_env *env, int32_t id, const f
 int vrg_env_add_triangles(vrg_env *env, const float *xyz, const int32_t *ids, int64_t n);
 
 /* The lumps of a compiled map that addBrushesForRayTrace reads
- * (cmd/tasks/loadbsp/main.go:284-340), as arrays the caller has parsed
+ * (cmd/tasks/loadbsp/main.go:283-340), as arrays the caller has parsed
  * (lump records reduced to the fields used; counts are record counts).
  * planes: num_planes x {normal xyz, dist}, in the BSP's pairs (p ^ 1 is p
  * facing the other way); node_children: num_nodes x {child0, child1}
@@ -193,7 +193,7 @@ typedef struct vrg_bsp_world {
     int32_t first_face;
     int32_t num_model_faces;
 } vrg_bsp_world;
-/* addBrushesForRayTrace (cmd/tasks/loadbsp/main.go:284-340) and
+/* addBrushesForRayTrace (cmd/tasks/loadbsp/main.go:283-340) and
  * addBrushToRaytraceEnvironment (:241-282): every opaque brush (contents &
  * VRG_MASK_OPAQUE) of the world, in GetBrushRecursive order (brush.go:7-36),
  * adds each side that is neither sky nor a displacement as the fan of its
@@ -207,7 +207,7 @@ typedef struct vrg_bsp_world {
  * triangles added may be returned (NULL to skip). */
 int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *brush_triangles,
                           int64_t *sky_triangles);
-/* BaseWindingForPlane (vmath/polygon/winding.go:26-83): the quad
+/* BaseWindingForPlane (vmath/polygon/winding.go:25-83): the quad
  * (4 x xyz) of half-side 65536 on the plane, around normal * dist. */
 int vrg_base_winding_for_plane(const float *normal, float dist, float *out12);
 /* ChopWindingInPlace (winding.go:85-170): the part of the n-point winding

@@ -1711,12 +1711,12 @@ int orc_calc_face_extents(const float *verts, int32_t nverts, const float *vecs,
 /* ---- brush ingest (fixed mode) ----
  * addBrushesForRayTrace / addBrushToRaytraceEnvironment
  * (cmd/tasks/loadbsp/main.go:241-340), BaseWindingForPlane and
- * ChopWindingInPlace (vmath/polygon/winding.go:26-170), with the defects the
+ * ChopWindingInPlace (vmath/polygon/winding.go:25-170), with the defects the
  * fixed mode repairs: sky sides are skipped (the reference keeps only them,
  * main.go:255); the major axis reads normal[i] and axes 0 and 1 share the
  * up vector (0,0,1) (winding.go:36,45-51); the fourth point is written
  * (winding.go:77-78); the wrap-around side/distance entry is set and the
- * split loop advances j (winding.go:100-114,148).  No literal mode: the Go
+ * split loop advances j (winding.go:112,149).  No literal mode: the Go
  * as written never leaves the split loop. */
 #define ORC_WPTS 68
 

@@ -21,7 +21,7 @@
  *   common/types/patch.go, transfer.go         patch / transfer layout
  *   rad/world/face.go:14-90                    face lightmap extents
  *   cmd/tasks/loadbsp/main.go:241-340          brushes and sky faces -> triangles
- *   vmath/polygon/winding.go:26-170            base winding, winding chop
+ *   vmath/polygon/winding.go:25-170            base winding, winding chop
  * Gather, transfer building and the bounce loop are absent from the
  * reference; their semantics are the project's own and are written out in
  * the comments of vrad_oracle.c beside each function.

@@ -2,7 +2,7 @@
 // environment: addBrushesForRayTrace / addBrushToRaytraceEnvironment
 // (cmd/tasks/loadbsp/main.go:241-340) over lump arrays the caller has parsed
 // (the reference reads them through galaco/bsp, which is not part of it), with
-// BaseWindingForPlane and ChopWindingInPlace (vmath/polygon/winding.go:26-170).
+// BaseWindingForPlane and ChopWindingInPlace (vmath/polygon/winding.go:25-170).
 //
 // Behaviour kept from the reference, with these defects fixed:
 //   - brush sides: the reference skips every side WITHOUT SURF_SKY (the test
@@ -10,13 +10,13 @@
 //     sky sides and displacement sides are skipped and the rest are added;
 //   - BaseWindingForPlane reads normal[1] for every axis when it picks the
 //     major axis (winding.go:36), its Go switch has no fallthrough so axis 0
-//     gets a zero up vector (winding.go:45-51), and it writes Points[0] where
+//     gets a zero up vector (winding.go:46-52), and it writes Points[0] where
 //     Points[3] is meant (winding.go:77-78);
 //   - ChopWindingInPlace never sets the wrap-around entry sides[n] = sides[0]
-//     (its loop variable shadows the outer i, winding.go:100-114) and its
-//     split-point loop advances i instead of j (winding.go:148);
+//     (its loop variable shadows the outer i, winding.go:112) and its
+//     split-point loop advances i instead of j (winding.go:149);
 //   - the vertex index of a sky face is checked against the vertex count, not
-//     the edge count (main.go:318).
+//     the edge count (main.go:328-329).
 // Arithmetic is float32, one rounding per operation in the order written
 // (mgl32's Dot, Cross, Normalize as published: sums left to right,
 // 1 / sqrt of the squared length).
@@ -167,7 +167,7 @@ int check_world(const vrg_bsp_world &w) {
         const int32_t *f = w.faces + 3 * (int64_t)(w.first_face + k);
         if (f[0] < 0 || f[1] < 0 || (int64_t)f[0] + f[1] > w.num_surf_edges || f[2] >= w.num_texinfo)
             return VRG_ERR_INVALID;
-        if (f[1] > kMaxWindingPoints) return VRG_ERR_INVALID;  // main.go:305-307
+        if (f[1] > kMaxWindingPoints) return VRG_ERR_INVALID;  // main.go:311-313
         if (((f[2] >= 0 ? w.texinfo_flags[f[2]] : 0) & VRG_SURF_SKY) == 0) continue;
         for (int32_t j = 0; j < f[1]; j++) {
             const int64_t e = w.surf_edges[f[0] + j];
@@ -293,7 +293,7 @@ int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *bru
         }
         for (int32_t j = 2; j < f[1]; j++) put(pts[0], pts[j - 1], pts[j], VRG_TRACE_ID_SKY);
     }
-    const float coverage[3] = {1.0f, 0.0f, 0.0f};  // fullCoverage, main.go:270,334
+    const float coverage[3] = {1.0f, 0.0f, 0.0f};  // fullCoverage, main.go:275,337
     for (size_t t = 0; t < ids.size(); t++) {
         const float *p = xyz.data() + 9 * t;
         const int rc = vrg_env_add_triangle(env, ids[t], p, p + 3, p + 6, coverage, 0, 0);

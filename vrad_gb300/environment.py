@@ -182,7 +182,7 @@ class BspWorld(C.Structure):
 
 
 def base_winding_for_plane(normal, dist):
-    """BaseWindingForPlane (vmath/polygon/winding.go:26-83): 4 x 3 float32."""
+    """BaseWindingForPlane (vmath/polygon/winding.go:25-83): 4 x 3 float32."""
     lib = _lib.load()
     out = np.zeros((4, 3), np.float32)
     check(lib.vrg_base_winding_for_plane(_p(_f32(normal, (3,))), float(dist), _p(out)), None,
@@ -275,7 +275,7 @@ class Environment:
 
     def add_bsp_world(self, lumps: dict, headnode: int = 0, first_face: int = 0,
                       num_model_faces: int | None = None):
-        """addBrushesForRayTrace (cmd/tasks/loadbsp/main.go:284-340): the world's
+        """addBrushesForRayTrace (cmd/tasks/loadbsp/main.go:283-340): the world's
         opaque brushes and sky faces as triangles; returns (brush, sky) counts."""
         w, keep = BspWorld.from_arrays(lumps, headnode, first_face, num_model_faces)
         nb, ns = C.c_int64(), C.c_int64()
