@@ -31,7 +31,7 @@ namespace vrg {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;
 
 // Bit pattern of a channel after the clamp to [0, FLT_MAX].
 __device__ __forceinline__ uint32_t channel_bits(float c) {
@@ -61,36 +61,36 @@ __device__ __forceinline__ uint32_t encode_sample(float r, float g, float b) {
            ((uint32_t)(uint8_t)(int8_t)x << 24);
 }
 
-// One thread per luxel (grid-stride); reads 12 bytes of direct light, a
-// face record and a few patch nodes (L1/L2), writes one 4-byte sample.
+// One block per face (grid-stride over faces): every thread reads the same
+// face record (one broadcast), the threads take the face's luxels in order
+// (coalesced 12-byte reads and 4-byte writes), and the face's patch-tree
+// nodes stay in L1 while its luxels descend them.  No luxel -> face search.
 __global__ void __launch_bounds__(kThreads) k_lightmap(
-    const FaceRec *__restrict__ faces, const int64_t *__restrict__ off, int nfaces, int64_t nlux,
+    const FaceRec *__restrict__ faces, const int64_t *__restrict__ off, int nfaces,
     const float *__restrict__ rgb, const float4 *__restrict__ total, const PatchNode *__restrict__ pnodes,
     const int32_t *__restrict__ face_root, uint32_t *__restrict__ out) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t lux = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; lux < nlux; lux += stride) {
-        const int f = find_face(off, nfaces, lux);
+    for (int f = blockIdx.x; f < nfaces; f += gridDim.x) {
         const FaceRec fr = faces[f];
-        const int64_t local = lux - __ldg(off + f);
-        const int iv = (int)(local / fr.nu);
-        const int iu = (int)(local - (int64_t)iv * fr.nu);
-        float r = __ldg(rgb + 3 * lux), g = __ldg(rgb + 3 * lux + 1), b = __ldg(rgb + 3 * lux + 2);
+        const int64_t base = __ldg(off + f);
+        const int64_t n = __ldg(off + f + 1) - base;
         const int32_t root = __ldg(face_root + f);
-        if (root >= 0) {
-            float px, py, pz;
-            luxel_sample(fr, lux, iu, iv, 0, 1, 0, px, py, pz);
-            int32_t node = root;
-            PatchNode pn = pnodes[node];
-            while (pn.axis >= 0) {
-                node = pick3(pn.axis, px, py, pz) >= pn.dist ? pn.child1 : pn.child2;
-                pn = pnodes[node];
+        for (int64_t local = threadIdx.x; local < n; local += blockDim.x) {
+            const int64_t lux = base + local;
+            const int iv = (int)(local / fr.nu);
+            const int iu = (int)(local - (int64_t)iv * fr.nu);
+            float r = __ldg(rgb + 3 * lux), g = __ldg(rgb + 3 * lux + 1), b = __ldg(rgb + 3 * lux + 2);
+            if (root >= 0) {
+                float px, py, pz;
+                luxel_sample(fr, lux, iu, iv, 0, 1, 0, px, py, pz);
+                PatchNode pn = pnodes[root];
+                while (pn.axis >= 0) pn = pnodes[pick3(pn.axis, px, py, pz) >= pn.dist ? pn.child1 : pn.child2];
+                const float4 t = total[pn.leaf];
+                r = radd(r, t.x);
+                g = radd(g, t.y);
+                b = radd(b, t.z);
             }
-            const float4 t = total[pn.leaf];
-            r = radd(r, t.x);
-            g = radd(g, t.y);
-            b = radd(b, t.z);
+            out[lux] = encode_sample(r, g, b);
         }
-        out[lux] = encode_sample(r, g, b);
     }
 }
 
@@ -114,11 +114,11 @@ int vrg_env_get_lightmap(vrg_env *env, uint8_t *samples, int64_t *face_offset) {
     if (!samples || nlux == 0) return VRG_OK;
     cudaStream_t st = ctx->stream;
     VRG_CUDA(ctx, env->d_out0.reserve(4 * (size_t)nlux));
-    const int grid = (int)std::min<int64_t>((nlux + kThreads - 1) / kThreads, (int64_t)ctx->num_sms * 8);
+    const int grid = (int)std::min<int64_t>(env->nfaces, (int64_t)ctx->num_sms * 16);
     cudaEvent_t ev = nullptr;
     timing_begin(ctx, "lightmap", &ev);
     k_lightmap<<<grid, kThreads, 0, st>>>(env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(),
-                                         env->nfaces, nlux, env->d_bake_rgb.as<float>(),
+                                         env->nfaces, env->d_bake_rgb.as<float>(),
                                          env->d_total.as<float4>(), env->d_patch_nodes.as<PatchNode>(),
                                          env->d_face_root.as<int32_t>(), env->d_out0.as<uint32_t>());
     VRG_CUDA(ctx, cudaGetLastError());
