@@ -207,6 +207,22 @@ typedef struct vrg_bsp_world {
  * triangles added may be returned (NULL to skip). */
 int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *brush_triangles,
                           int64_t *sky_triangles);
+/* A compiled map's bytes decoded into the lumps vrg_bsp_world names (the
+ * reference reads them through galaco/bsp, cmd/tasks/loadbsp/main.go:31-40).
+ * Source BSP versions 19-21, little-endian; leaf lump version 0 (56-byte
+ * leaves) or 1 (32-byte); compressed lumps give VRG_ERR_UNSUPPORTED, a bad
+ * magic, a lump outside the data or a lump that is not whole records
+ * VRG_ERR_INVALID.  The handle owns the decoded arrays; `data` is not kept. */
+typedef struct vrg_bsp vrg_bsp;
+int vrg_bsp_open(const uint8_t *data, size_t size, vrg_bsp **out);
+void vrg_bsp_close(vrg_bsp *bsp);
+/* Fills `world` with pointers into the handle's arrays (valid until
+ * vrg_bsp_close) and model 0's headnode and face range. */
+int vrg_bsp_get_world(const vrg_bsp *bsp, vrg_bsp_world *world);
+/* BSP version, texinfo count and the texinfos' LightmapVecsLuxelsPerWorldUnits
+ * (8 floats each, for vrg_calc_face_extents); any pointer may be NULL. */
+int vrg_bsp_info(const vrg_bsp *bsp, int32_t *version, int32_t *num_texinfo,
+                 const float **lightmap_vecs);
 /* BaseWindingForPlane (vmath/polygon/winding.go:25-83): the quad
  * (4 x xyz) of half-side 65536 on the plane, around normal * dist. */
 int vrg_base_winding_for_plane(const float *normal, float dist, float *out12);

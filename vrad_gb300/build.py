@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_EXACT = ["trace.cu", "direct.cu", "transfer.cu", "batch.cu", "relight.cu", "lightmap.cu"]
 CU_FAST = ["bounce.cu", "kdbuild_gpu.cu"]
-CPP = ["capi.cpp", "environment.cpp", "kdbuild.cpp", "lights.cpp", "patches.cpp", "tune.cpp", "bsp.cpp"]
+CPP = ["capi.cpp", "environment.cpp", "kdbuild.cpp", "lights.cpp", "patches.cpp", "tune.cpp", "bsp.cpp", "bsp_file.cpp"]
 
 
 def _nvcc() -> str:

@@ -181,6 +181,34 @@ class BspWorld(C.Structure):
         return w, keep
 
 
+def read_bsp(data: bytes):
+    """Decodes a compiled map (vrg_bsp_open): the lump arrays the brush ingest
+    reads, keyed as BspWorld.from_arrays takes them, plus model 0's headnode and
+    face range, the BSP version and the texinfos' lightmap vectors."""
+    lib = _lib.load()
+    buf = np.frombuffer(data, np.uint8)
+    h = C.c_void_p()
+    check(lib.vrg_bsp_open(_p(buf) if buf.size else None, buf.size, C.byref(h)), None, "bsp_open")
+    try:
+        w = BspWorld()
+        check(lib.vrg_bsp_get_world(h, C.byref(w)), None, "bsp_get_world")
+        out = {}
+        for name, dt, per in BspWorld.LUMPS:
+            n = getattr(w, BspWorld.COUNTS[name]) * per
+            ptr = getattr(w, name)
+            ct = C.c_float if dt == np.float32 else C.c_int32
+            a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), (n,)).copy() if n else np.zeros(0, dt)
+            out[name] = a.reshape(-1, per)
+        version, ntex, vecs = C.c_int32(), C.c_int32(), C.POINTER(C.c_float)()
+        check(lib.vrg_bsp_info(h, C.byref(version), C.byref(ntex), C.byref(vecs)), None, "bsp_info")
+        lm = (np.ctypeslib.as_array(vecs, (ntex.value * 8,)).copy() if ntex.value
+              else np.zeros(0, np.float32)).reshape(-1, 2, 4)
+        return dict(lumps=out, headnode=w.headnode, first_face=w.first_face,
+                    num_model_faces=w.num_model_faces, version=version.value, lightmap_vecs=lm)
+    finally:
+        lib.vrg_bsp_close(h)
+
+
 def base_winding_for_plane(normal, dist):
     """BaseWindingForPlane (vmath/polygon/winding.go:25-83): 4 x 3 float32."""
     lib = _lib.load()
@@ -283,6 +311,11 @@ class Environment:
                   "add_bsp_world")
         del keep
         return nb.value, ns.value
+
+    def add_bsp_file(self, data: bytes):
+        """A compiled map's brushes and sky faces (vrg_bsp_open + vrg_env_add_bsp_world)."""
+        m = read_bsp(data)
+        return self.add_bsp_world(m["lumps"], m["headnode"], m["first_face"], m["num_model_faces"])
 
     def get_triangle_vertices(self, first: int = 0, n: int | None = None):
         """(n, 9) vertices and (n,) ids of the triangles added so far."""
