@@ -499,8 +499,8 @@ int vrg_env_bake(vrg_env *env, int32_t supersamples, uint64_t seed, int32_t max_
 int vrg_env_get_bake(vrg_env *env, float *luxel_rgb, float *patch_direct, float *patch_total, int32_t *bounces,
                      float *delta) {
     if (!env) return VRG_ERR_INVALID;
-    if (!env->have_bake) return fail(env->ctx, VRG_ERR_STATE, "no bake has run on this scene");
     std::lock_guard<std::mutex> lk(env->mu);
+    if (!env->have_bake) return fail(env->ctx, VRG_ERR_STATE, "no bake of the current faces and patches has run on this scene");
     vrg_ctx *ctx = env->ctx;
     const int64_t nlux = env->luxel_offset.empty() ? 0 : env->luxel_offset.back();
     const int64_t nl = (int64_t)env->patches.leaf_patch.size();
