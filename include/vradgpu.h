@@ -3,7 +3,9 @@
  *
  * One shared library (libvradgpu.so) stands behind the reference's Go entry
  * points for the ray tracer, direct-light gathering, transfer building and
- * the bounce loop.  Plain pointers and sizes only; every call returns an int
+ * the bounce loop, and for the stages on either side: reading a compiled
+ * map's brushes into the ray tracer, and face extents and lightmap samples
+ * after the bake.  Plain pointers and sizes only; every call returns an int
  * status (VRG_OK = 0, negative on error) and the message of the most recent
  * failure on a context is available from vrg_last_error().
  *
