@@ -306,6 +306,21 @@ int vrg_env_occlusion_mask(vrg_env *env, const float *start, const float *stop, 
                            int32_t skip_id, uint32_t *out_mask, int32_t *out_hit, float *out_t);
 int vrg_env_occlusion_mask_d(vrg_env *env, const float *start, const float *stop, int64_t n,
                              int32_t skip_id, uint32_t *out_mask, int32_t *out_hit, float *out_t);
+/* CanLeafTraceToSky (rad/lightmap/lightmap.go:425-451) for n leaves given
+ * by their integer bounds (leaf_mins / leaf_maxs: n x 3, the BSP leaf's
+ * mins and maxs): from the centre (float)(mins + maxs) * 0.5, one shadow
+ * line per Anorms direction a_j (162) to a_j * -MAX_TRACE_LENGTH + centre
+ * (per component, float32), with TestLineDoesHitSky's semantics and no
+ * static prop skipped; out[i] = 1 when any line's fraction visible is above
+ * 0.  The reference traces from the origin (its centre vector is never
+ * loaded, lightmap.go:432) and its direction loader keeps only x
+ * (vmath/ssemath/fourvectors.go:15-28); here the lines leave the centre. */
+int vrg_env_can_leaf_trace_to_sky(vrg_env *env, const int32_t *leaf_mins, const int32_t *leaf_maxs,
+                                  int64_t n, uint8_t *out);
+/* The lines vrg_env_can_leaf_trace_to_sky traces (n x 162 starts and stops,
+ * 3 floats each, leaf-major).  Host only; needs no context. */
+int vrg_leaf_sky_lines(const int32_t *leaf_mins, const int32_t *leaf_maxs, int64_t n, float *starts,
+                       float *stops);
 /* Ray stream (AddToRayStream / FlushStreamEntry / FinishRayStream,
  * environment.go:162-175): lines are queued on the host, traced in large
  * batches, and their fraction_visible values are returned in queue order. */

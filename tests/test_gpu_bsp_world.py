@@ -60,3 +60,21 @@ def test_brush_world_traces_like_the_oracle(gpu_ctx, oracle):
     frac = env.test_line_does_hit_sky(a[::4], b[::4])
     rfrac = oracle.Scene(xyz, ids).test_lines(a[::4], b[::4], threads=16)
     assert np.array_equal(frac, rfrac) and 0 < frac.mean() < 1
+
+
+def test_can_leaf_trace_to_sky_like_the_oracle(gpu_ctx, oracle):
+    from vrad_gb300.environment import Environment, leaf_sky_lines
+
+    env = Environment(gpu_ctx)
+    env.add_bsp_world(brush_room(seed=3))
+    env.SetupAccelerationStructure()
+    xyz, ids = env.get_triangle_vertices()
+    rng = np.random.default_rng(4)
+    mins = rng.integers(20, 1900, (300, 3)).astype(np.int32)
+    maxs = (mins + rng.integers(1, 120, (300, 3))).astype(np.int32)
+    mins[:20, 2], maxs[:20, 2] = -12, -4  # centres inside the solid floor: every line is stopped
+    got = env.CanLeafTraceToSky(mins, maxs)
+    a, b = leaf_sky_lines(mins, maxs)
+    frac = oracle.Scene(xyz, ids).test_lines(a, b, skip=-1, threads=16)
+    want = (frac.reshape(-1, 162) > 0).any(axis=1)
+    assert np.array_equal(got, want) and not want[:20].any() and want[20:].mean() > 0.5

@@ -88,6 +88,8 @@ SIGNATURES = {
     "vrg_base_winding_for_plane": (C.c_int, [P, F, P]),
     "vrg_chop_winding": (C.c_int, [P, I32, P, F, F, P, P]),
     "vrg_env_get_triangle_vertices": (C.c_int, [P, I64, I64, P, P]),
+    "vrg_env_can_leaf_trace_to_sky": (C.c_int, [P, P, P, I64, P]),
+    "vrg_leaf_sky_lines": (C.c_int, [P, P, I64, P, P]),
     "vrg_bsp_open": (C.c_int, [P, C.c_size_t, P]),
     "vrg_bsp_close": (None, [P]),
     "vrg_bsp_get_world": (C.c_int, [P, P]),

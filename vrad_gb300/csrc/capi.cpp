@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 
+#include "anorms_table.h"
 #include "vrg_internal.h"
 
 namespace vrg {
@@ -446,6 +447,50 @@ int vrg_env_test_line_does_hit_sky(vrg_env *env, const float *start, const float
     TRY(launch_test_lines(env, d_start, d_stop, n, skip, env->d_out0.as<float>()));
     TRY(download(ctx, fraction_visible, env->d_out0, 4 * n));
     return sync(ctx);
+}
+
+/* CanLeafTraceToSky (rad/lightmap/lightmap.go:425-451) */
+
+int vrg_leaf_sky_lines(const int32_t *leaf_mins, const int32_t *leaf_maxs, int64_t n, float *starts,
+                       float *stops) {
+    if (n < 0 || (n > 0 && (!leaf_mins || !leaf_maxs || !starts || !stops))) return VRG_ERR_INVALID;
+    static const float anorms[kNumAnorms * 3] = VRG_ANORMS_INIT;
+    const float scale = -kMaxTraceLength;
+    for (int64_t i = 0; i < n; i++) {
+        float c[3];
+        for (int a = 0; a < 3; a++) c[a] = (float)(leaf_mins[3 * i + a] + leaf_maxs[3 * i + a]) * 0.5f;
+        for (int j = 0; j < kNumAnorms; j++) {
+            float *st = starts + 3 * (i * kNumAnorms + j), *sp = stops + 3 * (i * kNumAnorms + j);
+            for (int a = 0; a < 3; a++) {
+                st[a] = c[a];
+                sp[a] = anorms[3 * j + a] * scale + c[a];
+            }
+        }
+    }
+    return VRG_OK;
+}
+
+int vrg_env_can_leaf_trace_to_sky(vrg_env *env, const int32_t *leaf_mins, const int32_t *leaf_maxs, int64_t n,
+                                  uint8_t *out) {
+    TRY(need_built(env));
+    if (n < 0 || (n > 0 && (!leaf_mins || !leaf_maxs || !out))) return VRG_ERR_INVALID;
+    constexpr int64_t kChunk = 4096;  // leaves per trace call: 663,552 lines, 16 MB of end points
+    std::vector<float> a, b, frac;
+    for (int64_t i0 = 0; i0 < n; i0 += kChunk) {
+        const int64_t m = std::min(kChunk, n - i0);
+        const int64_t lines = m * kNumAnorms;
+        a.resize(3 * lines);
+        b.resize(3 * lines);
+        frac.resize(lines);
+        TRY(vrg_leaf_sky_lines(leaf_mins + 3 * i0, leaf_maxs + 3 * i0, m, a.data(), b.data()));
+        TRY(vrg_env_test_line_does_hit_sky(env, a.data(), b.data(), lines, -1, frac.data()));
+        for (int64_t i = 0; i < m; i++) {
+            uint8_t sky = 0;
+            for (int j = 0; j < kNumAnorms && !sky; j++) sky = frac[i * kNumAnorms + j] > 0.0f ? 1 : 0;
+            out[i0 + i] = sky;
+        }
+    }
+    return VRG_OK;
 }
 
 /* ray stream: queue on the host, trace on finish in one batch */

@@ -209,6 +209,18 @@ def read_bsp(data: bytes):
         lib.vrg_bsp_close(h)
 
 
+def leaf_sky_lines(leaf_mins, leaf_maxs):
+    """The (n * 162) start and stop points CanLeafTraceToSky traces for each leaf."""
+    lib = _lib.load()
+    mn = np.ascontiguousarray(leaf_mins, np.int32).reshape(-1, 3)
+    mx = np.ascontiguousarray(leaf_maxs, np.int32).reshape(-1, 3)
+    n = mn.shape[0]
+    a = np.zeros((n * 162, 3), np.float32)
+    b = np.zeros((n * 162, 3), np.float32)
+    check(lib.vrg_leaf_sky_lines(_p(mn), _p(mx), n, _p(a), _p(b)), None, "leaf_sky_lines")
+    return a, b
+
+
 def base_winding_for_plane(normal, dist):
     """BaseWindingForPlane (vmath/polygon/winding.go:25-83): 4 x 3 float32."""
     lib = _lib.load()
@@ -410,6 +422,15 @@ class Environment:
                                                           static_prop_to_skip, _p(out)),
                   "TestLineDoesHitSky")
         return out
+
+    def CanLeafTraceToSky(self, leaf_mins, leaf_maxs):
+        """rad/lightmap/lightmap.go:425-451 for every leaf: bool per leaf."""
+        mn = np.ascontiguousarray(leaf_mins, np.int32).reshape(-1, 3)
+        mx = np.ascontiguousarray(leaf_maxs, np.int32).reshape(-1, 3)
+        out = np.zeros(mn.shape[0], np.uint8)
+        self._chk(self.lib.vrg_env_can_leaf_trace_to_sky(self.h, _p(mn), _p(mx), mn.shape[0],
+                                                         _p(out)), "CanLeafTraceToSky")
+        return out.astype(bool)
 
     def occlusion_mask(self, start, stop, skip_id=-1, closest=False):
         a, b = _f32(start, (-1, 3)), _f32(stop, (-1, 3))
