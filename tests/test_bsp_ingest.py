@@ -258,3 +258,30 @@ def test_rejected_input_adds_nothing(vlib, host_ctx):
     env.SetupAccelerationStructure()
     with pytest.raises(VrgError):  # after the build
         env.add_bsp_world(good)
+
+
+def test_many_brushes_keep_the_reference_order(vlib, host_ctx, oracle):
+    """Enough brushes for the ingest to split the list over threads: the
+    triangles still come out in the BSP walk's order, bit for bit."""
+    rng = np.random.default_rng(12)
+    w = World()
+    for k in range(3000):
+        c = rng.uniform(0, 8000, 3)
+        if k % 7 == 0:
+            n = rng.normal(size=(6, 3))
+            n = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+            planes = [(n[i], float(np.float32(n[i].astype(np.float64) @ c + 40))) for i in range(6)]
+            for a in range(3):
+                e = np.zeros(3, np.float32)
+                e[a] = 1
+                planes += [(e, float(c[a] + 60)), (-e, float(-(c[a] - 60)))]
+            w.brush(planes, contents=CONTENTS_SOLID if k % 11 else CONTENTS_WATER)
+        else:
+            e = rng.uniform(4, 100, 3)
+            w.box(c - e, c + e, texinfo={int(k % 6): 1} if k % 5 == 0 else None)
+    order = rng.permutation(3000)
+    leaves = [list(order[i:i + 37]) for i in range(0, 3000, 37)]
+    lumps = w.lumps(leaves=leaves)
+    env, xyz, ids, nb, ns = _ingest(host_ctx, lumps)
+    rx, rids, rnb = oracle.bsp_world_triangles(lumps)
+    assert nb == rnb > 30000 and np.array_equal(xyz, rx) and np.array_equal(ids, rids)

@@ -20,8 +20,11 @@
 // Arithmetic is float32, one rounding per operation in the order written
 // (mgl32's Dot, Cross, Normalize as published: sums left to right,
 // 1 / sqrt of the squared length).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "vrg_internal.h"
@@ -67,18 +70,24 @@ void base_winding(const float *n, float dist, V3 *out) {
     out[3] = V3{(org.x - right.x) - up.x, (org.y - right.y) - up.y, (org.z - right.z) - up.z};
 }
 
+// A winding with room for the limit plus the points one chop can add.
+struct Winding {
+    V3 p[kMaxWindingPoints + 4];
+    int n = 0;
+};
+
 // Keeps the part of w in front of the plane (n . p - dist > -epsilon).
 // Returns 0 with w emptied when nothing is in front, -1 when the result would
 // pass the winding limit.
-int chop_winding(std::vector<V3> &w, const float *n, float dist, float epsilon) {
-    const int np = (int)w.size();
+int chop_winding(Winding &w, const float *n, float dist, float epsilon) {
+    const int np = w.n;
     if (np == 0) return 0;
     const V3 N{n[0], n[1], n[2]};
-    std::vector<float> dists(np + 1);
-    std::vector<int> sides(np + 1);
+    float dists[kMaxWindingPoints + 5];
+    int sides[kMaxWindingPoints + 5];
     int counts[3] = {0, 0, 0};
     for (int i = 0; i < np; i++) {
-        const float d = dot(w[i], N) - dist;
+        const float d = dot(w.p[i], N) - dist;
         dists[i] = d;
         sides[i] = d > epsilon ? kFront : (d < -epsilon ? kBack : kOn);
         counts[sides[i]]++;
@@ -86,21 +95,21 @@ int chop_winding(std::vector<V3> &w, const float *n, float dist, float epsilon) 
     sides[np] = sides[0];
     dists[np] = dists[0];
     if (counts[kFront] == 0) {
-        w.clear();
+        w.n = 0;
         return 0;
     }
     if (counts[kBack] == 0) return 0;
-    std::vector<V3> f;
-    f.reserve(np + 4);
+    Winding f;
     for (int i = 0; i < np; i++) {
-        const V3 &p1 = w[i];
+        const V3 &p1 = w.p[i];
+        if (f.n > kMaxWindingPoints + 2) return -1;  // room for the two pushes below
         if (sides[i] == kOn) {
-            f.push_back(p1);
+            f.p[f.n++] = p1;
             continue;
         }
-        if (sides[i] == kFront) f.push_back(p1);
+        if (sides[i] == kFront) f.p[f.n++] = p1;
         if (sides[i + 1] == kOn || sides[i + 1] == sides[i]) continue;
-        const V3 &p2 = w[(i + 1) % np];
+        const V3 &p2 = w.p[(i + 1) % np];
         const float t = dists[i] / (dists[i] - dists[i + 1]);
         const float a[3] = {p1.x, p1.y, p1.z}, b[3] = {p2.x, p2.y, p2.z};
         float m[3];
@@ -109,10 +118,10 @@ int chop_winding(std::vector<V3> &w, const float *n, float dist, float epsilon) 
             else if (n[j] == -1.0f) m[j] = -dist;
             else m[j] = a[j] + t * (b[j] - a[j]);
         }
-        f.push_back(V3{m[0], m[1], m[2]});
+        f.p[f.n++] = V3{m[0], m[1], m[2]};
     }
-    if ((int)f.size() > kMaxWindingPoints) return -1;
-    w.swap(f);
+    if (f.n > kMaxWindingPoints) return -1;
+    w = f;
     return 0;
 }
 
@@ -232,11 +241,12 @@ int vrg_base_winding_for_plane(const float *normal, float dist, float *out12) {
 int vrg_chop_winding(const float *points, int32_t n, const float *normal, float dist, float epsilon,
                      float *out, int32_t *out_n) {
     if (n < 0 || n > kMaxWindingPoints || (n && !points) || !normal || !out || !out_n) return VRG_ERR_INVALID;
-    std::vector<V3> w(n);
-    if (n) memcpy(w.data(), points, sizeof(V3) * (size_t)n);
+    Winding w;
+    w.n = n;
+    if (n) memcpy(w.p, points, sizeof(V3) * (size_t)n);
     if (chop_winding(w, normal, dist, epsilon) != 0) return VRG_ERR_UNSUPPORTED;
-    if (!w.empty()) memcpy(out, w.data(), sizeof(V3) * w.size());
-    *out_n = (int32_t)w.size();
+    if (w.n) memcpy(out, w.p, sizeof(V3) * (size_t)w.n);
+    *out_n = w.n;
     return VRG_OK;
 }
 
@@ -245,10 +255,6 @@ int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *bru
     if (!env || !world) return VRG_ERR_INVALID;
     const vrg_bsp_world &w = *world;
     if (check_world(w) != VRG_OK) return fail(env->ctx, VRG_ERR_INVALID, "BSP lumps hold an index out of range or a non-finite value");
-    {
-        std::lock_guard<std::mutex> lk(env->mu);
-        if (env->built) return fail(env->ctx, VRG_ERR_STATE, "triangles added after SetupAccelerationStructure");
-    }
     // build every triangle first, so a failure adds none
     std::vector<float> xyz;
     std::vector<int32_t> ids;
@@ -259,26 +265,64 @@ int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *bru
     };
     std::vector<int32_t> brushes;
     if (brush_list(w, brushes) != VRG_OK) return fail(env->ctx, VRG_ERR_INVALID, "BSP nodes do not form a tree");
-    for (const int32_t bi : brushes) {
-        const int32_t *b = w.brushes + 3 * bi;
-        if ((b[2] & VRG_MASK_OPAQUE) == 0) continue;
-        for (int32_t i = 0; i < b[1]; i++) {
-            const int32_t *side = w.brush_sides + 4 * (b[0] + i);
-            const int32_t tflags = side[1] >= 0 ? w.texinfo_flags[side[1]] : 0;
-            if ((tflags & VRG_SURF_SKY) != 0 || side[2] != 0) continue;
-            const float *pl = w.planes + 4 * side[0];
-            std::vector<V3> poly(4);
-            base_winding(pl, pl[3], poly.data());
-            for (int32_t j = 0; j < b[1] && !poly.empty(); j++) {
-                if (j == i) continue;
-                const int32_t *other = w.brush_sides + 4 * (b[0] + j);
-                if (other[3] != 0) continue;  // bevel
-                const float *op = w.planes + 4 * (other[0] ^ 1);
-                if (chop_winding(poly, op, op[3], 0.0f) != 0)
-                    return fail(env->ctx, VRG_ERR_UNSUPPORTED, "brush side winding passed 64 points");
+    // Brushes are independent: contiguous runs of the list go to threads,
+    // each filling its own triangle list, joined in list order afterwards.
+    const int64_t nb = (int64_t)brushes.size();
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nth = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hw, 16, nb / 256}));
+    std::vector<std::vector<float>> part_xyz(nth);
+    std::vector<int64_t> part_tris(nth, 0);
+    std::vector<int> part_rc(nth, 0);
+    auto run = [&](int t) {
+        const int64_t b0 = nb * t / nth, b1 = nb * (t + 1) / nth;
+        std::vector<float> &out = part_xyz[t];
+        Winding poly;
+        for (int64_t k = b0; k < b1; k++) {
+            const int32_t *b = w.brushes + 3 * brushes[k];
+            if ((b[2] & VRG_MASK_OPAQUE) == 0) continue;
+            for (int32_t i = 0; i < b[1]; i++) {
+                const int32_t *side = w.brush_sides + 4 * (b[0] + i);
+                const int32_t tflags = side[1] >= 0 ? w.texinfo_flags[side[1]] : 0;
+                if ((tflags & VRG_SURF_SKY) != 0 || side[2] != 0) continue;
+                const float *pl = w.planes + 4 * side[0];
+                poly.n = 4;
+                base_winding(pl, pl[3], poly.p);
+                for (int32_t j = 0; j < b[1] && poly.n > 0; j++) {
+                    if (j == i) continue;
+                    const int32_t *other = w.brush_sides + 4 * (b[0] + j);
+                    if (other[3] != 0) continue;  // bevel
+                    const float *op = w.planes + 4 * (other[0] ^ 1);
+                    if (chop_winding(poly, op, op[3], 0.0f) != 0) {
+                        part_rc[t] = 1;
+                        return;
+                    }
+                }
+                for (int j = 2; j < poly.n; j++) {
+                    const V3 *v[3] = {&poly.p[0], &poly.p[j - 1], &poly.p[j]};
+                    for (const V3 *q : v) {
+                        out.push_back(q->x);
+                        out.push_back(q->y);
+                        out.push_back(q->z);
+                    }
+                    part_tris[t]++;
+                }
             }
-            for (size_t j = 2; j < poly.size(); j++) put(poly[0], poly[j - 1], poly[j], VRG_TRACE_ID_OPAQUE);
         }
+    };
+    try {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nth; t++) pool.emplace_back(run, t);
+        run(0);
+        for (auto &th : pool) th.join();
+    } catch (const std::bad_alloc &) {
+        return fail(env->ctx, VRG_ERR_NOMEM, "out of host memory in the brush ingest");
+    } catch (const std::system_error &) {
+        return fail(env->ctx, VRG_ERR_NOMEM, "could not start the brush ingest threads");
+    }
+    for (int t = 0; t < nth; t++) {
+        if (part_rc[t]) return fail(env->ctx, VRG_ERR_UNSUPPORTED, "brush side winding passed 64 points");
+        xyz.insert(xyz.end(), part_xyz[t].begin(), part_xyz[t].end());
+        ids.insert(ids.end(), (size_t)part_tris[t], VRG_TRACE_ID_OPAQUE);
     }
     const int64_t nbrush = (int64_t)ids.size();
     for (int32_t k = 0; k < w.num_model_faces; k++) {
@@ -293,11 +337,22 @@ int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *bru
         }
         for (int32_t j = 2; j < f[1]; j++) put(pts[0], pts[j - 1], pts[j], VRG_TRACE_ID_SKY);
     }
-    const float coverage[3] = {1.0f, 0.0f, 0.0f};  // fullCoverage, main.go:275,337
-    for (size_t t = 0; t < ids.size(); t++) {
-        const float *p = xyz.data() + 9 * t;
-        const int rc = vrg_env_add_triangle(env, ids[t], p, p + 3, p + 6, coverage, 0, 0);
-        if (rc != VRG_OK) return rc;
+    // AddTriangle (environment.go:41-43) for each, in one append: flags 0,
+    // material 0, colour fullCoverage = (1, 0, 0) (main.go:275,337)
+    {
+        std::lock_guard<std::mutex> lk(env->mu);
+        if (env->built) return fail(env->ctx, VRG_ERR_STATE, "triangles added after SetupAccelerationStructure");
+        const size_t n = ids.size();
+        env->xyz.insert(env->xyz.end(), xyz.begin(), xyz.end());
+        env->ids.insert(env->ids.end(), ids.begin(), ids.end());
+        env->flags.insert(env->flags.end(), n, 0);
+        env->materials.insert(env->materials.end(), n, 0);
+        env->colours.reserve(env->colours.size() + 3 * n);
+        for (size_t t = 0; t < n; t++) {
+            env->colours.push_back(1.0f);
+            env->colours.push_back(0.0f);
+            env->colours.push_back(0.0f);
+        }
     }
     if (brush_triangles) *brush_triangles = nbrush;
     if (sky_triangles) *sky_triangles = (int64_t)ids.size() - nbrush;
