@@ -309,7 +309,7 @@ int64_t vrg_env_num_triangles(const vrg_env *env) { return env ? (int64_t)env->i
 
 int vrg_env_get_triangle_vertices(const vrg_env *env, int64_t first, int64_t n, float *xyz, int32_t *ids) {
     if (!env || first < 0 || n < 0 || (n && !xyz && !ids)) return VRG_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(const_cast<vrg_env *>(env)->mu);
+    std::lock_guard<std::mutex> lk(env->mu);
     if (first + n > (int64_t)env->ids.size()) return VRG_ERR_INVALID;
     if (xyz && n) memcpy(xyz, env->xyz.data() + 9 * first, sizeof(float) * 9 * (size_t)n);
     if (ids && n) memcpy(ids, env->ids.data() + first, sizeof(int32_t) * (size_t)n);

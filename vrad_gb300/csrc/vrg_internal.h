@@ -120,7 +120,7 @@ struct PatchSet {
 
 struct vrg_env {
     vrg_ctx *ctx = nullptr;
-    std::mutex mu;
+    mutable std::mutex mu;  // const readers (tree and triangle getters) lock it too
 
     // Environment fields (raytracer/environment.go:28-39)
     std::vector<float> xyz;  // 9 per triangle (TriGeometryData.VertexCoordData)
