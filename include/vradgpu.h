@@ -214,13 +214,19 @@ int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *bru
  * Source BSP versions 19-21, little-endian; leaf lump version 0 (56-byte
  * leaves) or 1 (32-byte); compressed lumps give VRG_ERR_UNSUPPORTED, a bad
  * magic, a lump outside the data or a lump that is not whole records
- * VRG_ERR_INVALID.  The handle owns the decoded arrays; `data` is not kept. */
+ * VRG_ERR_INVALID.  The handle owns the decoded arrays; `data` is not
+ * kept. */
 typedef struct vrg_bsp vrg_bsp;
 int vrg_bsp_open(const uint8_t *data, size_t size, vrg_bsp **out);
 void vrg_bsp_close(vrg_bsp *bsp);
 /* Fills `world` with pointers into the handle's arrays (valid until
  * vrg_bsp_close) and model 0's headnode and face range. */
 int vrg_bsp_get_world(const vrg_bsp *bsp, vrg_bsp_world *world);
+/* The world's faces from the HDR face lump (58) instead of lump 7, as
+ * loadbsp picks its target faces with -hdr (cmd/tasks/loadbsp/main.go:80-88).
+ * A face lump shorter than model 0's face range makes vrg_env_add_bsp_world
+ * refuse the world (the reference would index past it). */
+int vrg_bsp_use_hdr_faces(vrg_bsp *bsp, int32_t hdr);
 /* BSP version, texinfo count and the texinfos' LightmapVecsLuxelsPerWorldUnits
  * (8 floats each, for vrg_calc_face_extents); any pointer may be NULL. */
 int vrg_bsp_info(const vrg_bsp *bsp, int32_t *version, int32_t *num_texinfo,

@@ -13,10 +13,11 @@ from test_bsp_ingest import World
 
 PLANES, VERTEXES, NODES, TEXINFO, FACES, LEAFS = 1, 3, 5, 6, 7, 10
 EDGES, SURFEDGES, MODELS, LEAFBRUSHES, BRUSHES, BRUSHSIDES = 12, 13, 14, 17, 18, 19
+FACES_HDR = 58
 
 
 def write_bsp(lumps, headnode=0, first_face=0, num_faces=None, version=20, leaf_version=1,
-              lightmap_vecs=None, compressed=()):
+              lightmap_vecs=None, compressed=(), faces_hdr=None):
     """Bytes of a BSP file holding the given lump arrays (other lumps empty)."""
     a = {k: np.asarray(v) for k, v in lumps.items()}
     n_faces = len(a["faces"]) if num_faces is None else num_faces
@@ -29,9 +30,14 @@ def write_bsp(lumps, headnode=0, first_face=0, num_faces=None, version=20, leaf_
     vecs = (np.zeros((ntex, 2, 4)) if lightmap_vecs is None else np.asarray(lightmap_vecs))
     body[TEXINFO] = b"".join(struct.pack("<8f8f2i", *([0.25] * 8), *vecs[t].ravel(),
                                          int(a["texinfo_flags"][t]), 0) for t in range(ntex))
-    body[FACES] = b"".join(struct.pack("<HBBihhhh4BifiiiiiHHI", 0, 0, 0, int(f[0]), int(f[1]),
-                                       int(f[2]), -1, 0, 0, 255, 255, 255, 0, 1.0, 0, 0, 4, 4, -1,
-                                       0, 0, 0) for f in a["faces"].reshape(-1, 3))
+    def face_lump(faces):
+        return b"".join(struct.pack("<HBBihhhh4BifiiiiiHHI", 0, 0, 0, int(f[0]), int(f[1]), int(f[2]),
+                                    -1, 0, 0, 255, 255, 255, 0, 1.0, 0, 0, 4, 4, -1, 0, 0, 0)
+                        for f in np.asarray(faces).reshape(-1, 3))
+
+    body[FACES] = face_lump(a["faces"])
+    if faces_hdr is not None:
+        body[FACES_HDR] = face_lump(faces_hdr)
     leaves = []
     for first, n in a["leaf_brush_ranges"].reshape(-1, 2):
         rec = struct.pack("<ihh6h4Hh", 1, 0, 0, *([0] * 6), 0, 0, int(first), int(n), -1)
@@ -134,3 +140,23 @@ def test_malformed_files_are_rejected(vlib):
     for data in bad:
         with pytest.raises(VrgError):
             read_bsp(data)
+
+
+def test_hdr_faces(vlib, host_ctx):
+    from vrad_gb300._lib import VrgError
+    from vrad_gb300.environment import Environment, read_bsp
+
+    lumps = _world()
+    faces = np.asarray(lumps["faces"])
+    # the HDR lump holds only the pentagon; model 0 has one face
+    data = write_bsp(lumps, num_faces=1, faces_hdr=faces[2:3])
+    assert np.array_equal(read_bsp(data, hdr=True)["lumps"]["faces"], faces[2:3])
+    assert np.array_equal(read_bsp(data)["lumps"]["faces"], faces)
+    env = Environment(host_ctx)
+    assert env.add_bsp_file(data, hdr=True)[1] == 3  # the pentagon's fan
+    env = Environment(host_ctx)
+    assert env.add_bsp_file(data)[1] == 2  # LDR face 0: the square's fan
+    env = Environment(host_ctx)  # no HDR lump for model 0's face range: refused
+    with pytest.raises(VrgError):
+        env.add_bsp_file(write_bsp(lumps, num_faces=1), hdr=True)
+    assert env.num_triangles() == 0

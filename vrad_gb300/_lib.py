@@ -93,6 +93,7 @@ SIGNATURES = {
     "vrg_bsp_open": (C.c_int, [P, C.c_size_t, P]),
     "vrg_bsp_close": (None, [P]),
     "vrg_bsp_get_world": (C.c_int, [P, P]),
+    "vrg_bsp_use_hdr_faces": (C.c_int, [P, I32]),
     "vrg_bsp_info": (C.c_int, [P, P, P, P]),
     "vrg_batch_create": (C.c_int, [P, P]),
     "vrg_batch_destroy": (None, [P]),

@@ -32,6 +32,7 @@
 //   18 brushes     12 B  {int firstside, int numsides, int contents}
 //   19 brushsides   8 B  {u16 planenum, short texinfo, short dispinfo,
 //                         u8 bevel, u8 thin}
+//   58 faces (HDR)  56 B  as lump 7
 // Bytes are read with memcpy and assembled little-endian, so the decode is
 // the same on any host.
 #include <cstring>
@@ -42,9 +43,10 @@
 
 struct vrg_bsp {
     int32_t version = 0;
+    bool hdr = false;  // the world's faces from the HDR face lump
     std::vector<float> planes, vertexes;
     std::vector<int32_t> node_children, leaf_brush_ranges, leaf_brushes, brushes, brush_sides,
-        texinfo_flags, edges, surf_edges, faces;
+        texinfo_flags, edges, surf_edges, faces, faces_hdr;
     std::vector<float> lightmap_vecs;  // 8 per texinfo
     int32_t headnode = 0, first_face = 0, num_model_faces = 0;
 };
@@ -53,7 +55,8 @@ namespace {
 
 enum {
     kPlanes = 1, kVertexes = 3, kNodes = 5, kTexinfo = 6, kFaces = 7, kLeafs = 10, kEdges = 12,
-    kSurfEdges = 13, kModels = 14, kLeafBrushes = 17, kBrushes = 18, kBrushSides = 19, kNumLumps = 64
+    kSurfEdges = 13, kModels = 14, kLeafBrushes = 17, kBrushes = 18, kBrushSides = 19, kFacesHdr = 58,
+    kNumLumps = 64
 };
 constexpr size_t kHeaderBytes = 8 + 16 * kNumLumps + 4;
 
@@ -96,14 +99,14 @@ int vrg_bsp_open(const uint8_t *data, size_t size, vrg_bsp **out) {
         L[i] = Lump{data + ofs, (size_t)len, ri32(e + 8)};
         const bool used = i == kPlanes || i == kVertexes || i == kNodes || i == kTexinfo || i == kFaces ||
                           i == kLeafs || i == kEdges || i == kSurfEdges || i == kModels ||
-                          i == kLeafBrushes || i == kBrushes || i == kBrushSides;
+                          i == kLeafBrushes || i == kBrushes || i == kBrushSides || i == kFacesHdr;
         if (used && len > 0 && rd32(e + 12) != 0) return VRG_ERR_UNSUPPORTED;  // compressed lump
     }
     const size_t leaf_bytes = L[kLeafs].version == 0 ? 56 : 32;
     const struct {
         int lump;
         size_t rec;
-    } sizes[] = {{kPlanes, 20}, {kVertexes, 12}, {kNodes, 32}, {kTexinfo, 72}, {kFaces, 56},
+    } sizes[] = {{kPlanes, 20}, {kVertexes, 12}, {kNodes, 32}, {kTexinfo, 72}, {kFaces, 56}, {kFacesHdr, 56},
                  {kLeafs, leaf_bytes}, {kEdges, 4}, {kSurfEdges, 4}, {kModels, 48}, {kLeafBrushes, 2},
                  {kBrushes, 12}, {kBrushSides, 8}};
     for (const auto &s : sizes)
@@ -124,11 +127,14 @@ int vrg_bsp_open(const uint8_t *data, size_t size, vrg_bsp **out) {
             for (int k = 0; k < 8; k++) b->lightmap_vecs.push_back(rf32(t + 32 + 4 * k));
             b->texinfo_flags.push_back(ri32(t + 64));
         }
-        for (size_t i = 0; i < L[kFaces].bytes / 56; i++) {
-            const uint8_t *f = L[kFaces].p + 56 * i;
-            b->faces.push_back(ri32(f + 4));   // firstedge
-            b->faces.push_back(ri16(f + 8));   // numedges
-            b->faces.push_back(ri16(f + 10));  // texinfo
+        for (int lump : {kFaces, kFacesHdr}) {
+            std::vector<int32_t> &dst = lump == kFaces ? b->faces : b->faces_hdr;
+            for (size_t i = 0; i < L[lump].bytes / 56; i++) {
+                const uint8_t *f = L[lump].p + 56 * i;
+                dst.push_back(ri32(f + 4));   // firstedge
+                dst.push_back(ri16(f + 8));   // numedges
+                dst.push_back(ri16(f + 10));  // texinfo
+            }
         }
         for (size_t i = 0; i < L[kLeafs].bytes / leaf_bytes; i++) {
             const uint8_t *l = L[kLeafs].p + leaf_bytes * i;
@@ -186,11 +192,18 @@ int vrg_bsp_get_world(const vrg_bsp *b, vrg_bsp_world *w) {
     w->num_edges = (int32_t)(b->edges.size() / 2);
     w->surf_edges = p(b->surf_edges);
     w->num_surf_edges = (int32_t)b->surf_edges.size();
-    w->faces = p(b->faces);
-    w->num_faces = (int32_t)(b->faces.size() / 3);
+    const std::vector<int32_t> &faces = b->hdr ? b->faces_hdr : b->faces;
+    w->faces = p(faces);
+    w->num_faces = (int32_t)(faces.size() / 3);
     w->headnode = b->headnode;
     w->first_face = b->first_face;
     w->num_model_faces = b->num_model_faces;
+    return VRG_OK;
+}
+
+int vrg_bsp_use_hdr_faces(vrg_bsp *b, int32_t hdr) {
+    if (!b) return VRG_ERR_INVALID;
+    b->hdr = hdr != 0;
     return VRG_OK;
 }
 

@@ -181,7 +181,7 @@ class BspWorld(C.Structure):
         return w, keep
 
 
-def read_bsp(data: bytes):
+def read_bsp(data: bytes, hdr: bool = False):
     """Decodes a compiled map (vrg_bsp_open): the lump arrays the brush ingest
     reads, keyed as BspWorld.from_arrays takes them, plus model 0's headnode and
     face range, the BSP version and the texinfos' lightmap vectors."""
@@ -190,6 +190,7 @@ def read_bsp(data: bytes):
     h = C.c_void_p()
     check(lib.vrg_bsp_open(_p(buf) if buf.size else None, buf.size, C.byref(h)), None, "bsp_open")
     try:
+        check(lib.vrg_bsp_use_hdr_faces(h, int(hdr)), None, "bsp_use_hdr_faces")
         w = BspWorld()
         check(lib.vrg_bsp_get_world(h, C.byref(w)), None, "bsp_get_world")
         out = {}
@@ -324,9 +325,10 @@ class Environment:
         del keep
         return nb.value, ns.value
 
-    def add_bsp_file(self, data: bytes):
-        """A compiled map's brushes and sky faces (vrg_bsp_open + vrg_env_add_bsp_world)."""
-        m = read_bsp(data)
+    def add_bsp_file(self, data: bytes, hdr: bool = False):
+        """A compiled map's brushes and sky faces (vrg_bsp_open + vrg_env_add_bsp_world);
+        hdr takes the world's faces from the HDR face lump, as loadbsp does with -hdr."""
+        m = read_bsp(data, hdr)
         return self.add_bsp_world(m["lumps"], m["headnode"], m["first_face"], m["num_model_faces"])
 
     def get_triangle_vertices(self, first: int = 0, n: int | None = None):
