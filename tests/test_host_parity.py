@@ -28,6 +28,28 @@ def test_every_header_symbol_is_exported(vlib):
     assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
 
 
+def test_header_is_plain_c(tmp_path):
+    """The boundary header compiles as C99 and C11 with -pedantic, as a cgo
+    preamble or a C caller includes it."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = Path(__file__).resolve().parent.parent / "include"
+    src = tmp_path / "use.c"
+    src.write_text('#include "vradgpu.h"\n'
+                   "int main(void) { vrg_bsp_world w = {0}; vrg_light l = {0};\n"
+                   "  (void)w; (void)l; return VRG_OK; }\n")
+    for std in ("c99", "c11"):
+        r = subprocess.run([cc, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                            str(inc), "-c", str(src), "-o", str(tmp_path / "use.o")],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
 @pytest.mark.parametrize("which", ["anyhit", "lit", "random"])
 def test_kd_tree_matches_oracle(oracle, host_ctx, which, anyhit_scene, lit_scene):
     if which == "anyhit":
