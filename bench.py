@@ -1,14 +1,24 @@
 """Benchmark of the radiosity hot path on GB300.
 
-Default workload: the direct-light pass of a bake (4,096 box faces, 1.33M
+Headline (`value`): the direct-light pass of a bake (4,096 box faces, 1.33M
 luxels x 4 supersamples, 64 point + 8 spot lights + a 162-direction sky,
 8,208-triangle room whose ceiling is sky).  A step is one full gather; the
-metric is shadow rays traced per second (Mrays/s).  `--workload anyhit` runs
-the 2^20-line occlusion-mask case (12,300 triangles) instead.
+metric is shadow rays traced per second (Mrays/s), with the whole bake
+compared luxel by luxel against the oracle (`parity`).
 
-Prints ONE JSON line on rank 0.  `--impl reference` times the reference's
-CPU path instead: the C restatement of it under oracle/ (the Go reference has
-no toolchain here), with every host thread, on a bounded sample per step.
+The same JSON line carries the rest of the metric, one object per workload,
+each with its own error against the oracle and its roofline:
+  anyhit     2^20 shadow lines, 12,300 triangles: mask and closest-hit Mrays/s
+  radiosity  the same faces at 64-unit patches, 65,536 transfer rays per
+             patch: CSR build, bounce SpMV GB/s, solve to 1e-3
+  batch      256 scenes baked together vs one scene per launch: bakes/s
+  serve      8 resident scenes, Poisson relight requests: p50/p99 ms, bakes/s
+`--headline-only` skips them; `--workload X` prints one of them as its own
+line.
+
+`--impl reference` times the reference's CPU path instead: the C
+restatement of it under oracle/ (the Go reference has no toolchain here),
+with every host thread, on a bounded sample per step.
 """
 from __future__ import annotations
 
@@ -29,7 +39,6 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 SEED = 0
-CPU_SAMPLE_FACES = 1024  # bounded CPU baseline sample: faces [0, 1024) of 4,096
 STATS_SAMPLE_FACES = 256  # faces whose walk is counted for the byte model
 REF_FACES_PER_STEP = 256  # reference arm: faces per timed step
 
@@ -49,18 +58,55 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _ncu_traffic(kernel_file: str):
-    """DRAM bytes per launch from a committed ncu summary, if present."""
+def _profile_value(kernel_file: str, key: str):
+    """A `key: value` figure from a committed ncu summary under profiles/."""
     p = ROOT / "profiles" / kernel_file
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch_full:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def _ncu_traffic(kernel_file: str):
+    """DRAM bytes per launch from a committed ncu summary, if present."""
+    return _profile_value(kernel_file, "dram_bytes_per_launch_full")
+
+
+def rel_error_stats(got, ref, floor_frac=1e-3):
+    """Error of a device result against the oracle: share of bit-identical
+    values, max / p99 of |got - ref| / |ref| over ref != 0 (no floor), how
+    many ref == 0 values the device did not give as 0, and how many values
+    lie under floor_frac x max |ref| (counted, not excused)."""
+    g = np.ascontiguousarray(got, dtype=np.float32).ravel()
+    r = np.ascontiguousarray(ref, dtype=np.float32).ravel()
+    g64, r64 = g.astype(np.float64), r.astype(np.float64)
+    nz = r64 != 0.0
+    rel = np.abs(g64[nz] - r64[nz]) / np.abs(r64[nz])
+    top = float(np.abs(r64).max()) if r64.size else 0.0
+    return {"values": int(g.size),
+            "bit_identical": round(float(np.mean(g.view(np.uint32) == r.view(np.uint32))), 6),
+            "max_rel": float(rel.max()) if rel.size else 0.0,
+            "p99_rel": float(np.percentile(rel, 99)) if rel.size else 0.0,
+            "zero_ref_nonzero": int(np.count_nonzero(g64[~nz])),
+            f"under_{floor_frac:g}_of_max": int(np.count_nonzero(np.abs(r64) < floor_frac * top))}
+
+
+def issue_roofline(inst_per_unit, units, kernel_ms, sm_mhz, sms, source):
+    """Warp instructions issued per second against the SMs' issue rate (one
+    warp instruction per scheduler per cycle, 4 schedulers per SM)."""
+    if not inst_per_unit or not sm_mhz or not kernel_ms:
+        return None
+    achieved = inst_per_unit * units / (kernel_ms * 1e-3) / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"achieved": round(achieved, 1), "peak": round(peak, 1),
+            "unit": "G warp instructions/s", "frac": round(achieved / peak, 4),
+            "warp_instructions_per_unit": inst_per_unit, "sm_mhz": sm_mhz, "sms": sms,
+            "instructions_source": source}
 
 
 class Clocks:
@@ -159,7 +205,8 @@ def run_reference(args, rank):
         tot_t += t
     v = tot_r / tot_t / 1e6
     sample = (f"{REF_FACES_PER_STEP} of {nf} faces per step (~{tot_r // max(args.steps, 1)} "
-              f"shadow rays), 4 supersamples")
+              f"shadow rays), 4 supersamples; the walk is the reference's SAH tree "
+              f"(raytracer/environment.go:181-387) with no wall test")
     line = {
         "impl": "reference", "metric": "shadow Mrays/s (direct-light gather)", "value": round(v, 3),
         "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -202,11 +249,83 @@ def _l2_read_gbs(device: int):
     return gbs.value if rc == 0 else None
 
 
+def _admit(lib_ctx, xyz, ids):
+    """The scene's environment, and the time SetupAccelerationStructure takes
+    with the walk tree built on the GPU and on the host (ms; the GPU build is
+    timed after a first one that loads its kernels)."""
+    import torch
+
+    from vrad_gb300.environment import Environment
+
+    times = {}
+    for on_device in (1, 0, 1):
+        e = Environment(lib_ctx)
+        e.set_walk_tree_builder(on_device)
+        e.add_triangles(xyz, ids)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.SetupAccelerationStructure()
+        times["device" if on_device else "host"] = round((time.perf_counter() - t0) * 1e3, 2)
+        e.close()
+    e = Environment(lib_ctx)  # the default builder for this size
+    e.add_triangles(xyz, ids)
+    e.SetupAccelerationStructure()
+    return e, times
+
+
+def _event_ms(stream, fn, steps, flush):
+    """Per-step device times of fn (CUDA events on `stream`, L2 flushed
+    before each step)."""
+    import torch
+
+    out = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return out
+
+
+def _trace_roofline(kernel, units, avg_ms, bytes_per_unit, hbm_peak, hbm_kind, l2, clk, sms,
+                    prof, bytes_model, nodes, tris):
+    """Roofline record of a traversal kernel.  Its algorithmic bytes (kd
+    nodes and leaf records) are served from L1 and L2, so the governing roof
+    is instruction issue; the L2 and HBM fractions are given beside it, HBM
+    from the DRAM bytes ncu counted for the same kernel."""
+    alg = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
+    traffic = _ncu_traffic(prof)
+    sm_mhz = (clk or {}).get("sm_mhz")
+    issue = issue_roofline(_profile_value(prof, "warp_instructions_per_unit"), units, avg_ms,
+                           sm_mhz, sms, f"profiles/{prof}")
+    rec = {"bound": "issue", "kernel": kernel, "kernel_ms": round(avg_ms, 4),
+           "bytes_per_unit": round(bytes_per_unit, 2), "bytes_model": bytes_model,
+           "nodes_per_unit": round(float(nodes), 3), "tris_per_unit": round(float(tris), 3),
+           "l2": {"achieved": round(alg, 1), "peak": round(l2, 1) if l2 else None, "unit": "GB/s",
+                  "frac": round(alg / l2, 4) if l2 else None,
+                  "peak_source": "L2-resident read kernel (probe.cu), timed in this run"},
+           "hbm": {"achieved": round(traffic / (avg_ms * 1e-3) / 1e9, 1) if traffic else None,
+                   "peak": hbm_peak, "unit": "GB/s",
+                   "frac": round(traffic / (avg_ms * 1e-3) / 1e9 / hbm_peak, 5) if traffic else None,
+                   "peak_kind": f"{hbm_kind} HBM copy", "traffic_source": f"profiles/{prof}"},
+           "traffic": traffic}
+    if issue:
+        rec.update({"achieved": issue["achieved"], "peak": issue["peak"], "unit": issue["unit"],
+                    "frac": issue["frac"], "issue": issue})
+    else:
+        rec.update({"achieved": rec["l2"]["achieved"], "peak": rec["l2"]["peak"], "unit": "GB/s",
+                    "frac": rec["l2"]["frac"], "bound": "l2"})
+    return rec
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
 
     from vrad_gb300 import scenes
-    from vrad_gb300.environment import Context, Environment, light_array
+    from vrad_gb300.environment import Context, light_array
 
     dist = world > 1
     if dist:
@@ -223,83 +342,37 @@ def run_gpu(args, rank, world, local_rank):
     if args.autotune_file:
         lib_ctx.autotune_load(args.autotune_file)
     lib = lib_ctx.lib
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
 
-    def admit(xyz, ids):
-        """The scene's environment, and the time SetupAccelerationStructure
-        takes with the walk tree built on the GPU and on the host (ms; the
-        GPU build is timed after a first one that loads its kernels)."""
-        times = {}
-        for on_device in (1, 0, 1):
-            e = Environment(lib_ctx)
-            e.set_walk_tree_builder(on_device)
-            e.add_triangles(xyz, ids)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            e.SetupAccelerationStructure()
-            times["device" if on_device else "host"] = round((time.perf_counter() - t0) * 1e3, 2)
-            e.close()
-        e = Environment(lib_ctx)  # the default builder for this size
-        e.add_triangles(xyz, ids)
-        e.SetupAccelerationStructure()
-        return e, times
+    lit = scenes.lit_scene(SEED, n_faces=args.faces)
+    env, admit_ms = _admit(lib_ctx, lit.xyz, lit.ids)
+    env.set_faces(lit)
+    lights = light_array(lit.lights)
+    env.set_lights(lit.lights)
+    nlux = env.num_luxels()
+    d_out = torch.empty((nlux, 3), dtype=torch.float32, device=dev)
+    rays = C.c_uint64()
+    rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(), C.byref(rays))
+    assert rc == 0, rc
+    units = rays.value
+    kernel = "direct_luxels"
 
-    if args.workload == "anyhit":
-        sc = scenes.anyhit_scene(SEED)
-        env, admit_ms = admit(sc.xyz, sc.ids)
-        n = sc.starts.shape[0]
-        d_a = torch.from_numpy(sc.starts).to(dev)
-        d_b = torch.from_numpy(sc.stops).to(dev)
-        d_m = torch.empty((n + 31) // 32, dtype=torch.int32, device=dev)
-        units = n
-        kernel = "trace_mask"
-
-        def step_dev():
-            rc = lib.vrg_env_occlusion_mask_d(env.h, d_a.data_ptr(), d_b.data_ptr(), n, -1,
-                                              d_m.data_ptr(), None, None)
-            assert rc == 0, rc
-
-        h_a = torch.from_numpy(sc.starts).pin_memory()
-        h_b = torch.from_numpy(sc.stops).pin_memory()
-        h_m = torch.empty((n + 31) // 32, dtype=torch.int32).pin_memory()
-
-        def step_host():
-            rc = lib.vrg_env_occlusion_mask(env.h, h_a.data_ptr(), h_b.data_ptr(), n, -1,
-                                            h_m.data_ptr(), None, None)
-            assert rc == 0, rc
-
-        h2d, d2h = 24 * n, 4 * ((n + 31) // 32)
-        workload = "any-hit occlusion mask, 2^20 shadow lines, 12,300-triangle box room"
-        bytes_per_unit = None
-    else:
-        lit = scenes.lit_scene(SEED, n_faces=args.faces)
-        env, admit_ms = admit(lit.xyz, lit.ids)
-        env.set_faces(lit)
-        lights = light_array(lit.lights)
-        env.set_lights(lit.lights)
-        nlux = env.num_luxels()
-        d_out = torch.empty((nlux, 3), dtype=torch.float32, device=dev)
-        rays = C.c_uint64()
-        rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(), C.byref(rays))
+    def step_dev():
+        rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(), None)
         assert rc == 0, rc
-        units = rays.value
-        kernel = "direct_luxels"
 
-        def step_dev():
-            rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(), None)
-            assert rc == 0, rc
+    h_out = torch.empty((nlux, 3), dtype=torch.float32).pin_memory()
+    nl = len(lit.lights)
 
-        h_out = torch.empty((nlux, 3), dtype=torch.float32).pin_memory()
-        nl = len(lit.lights)
+    def step_host():
+        rc = lib.vrg_env_set_lights(env.h, lights, nl)
+        assert rc == 0, rc
+        rc = lib.vrg_env_gather_direct_light(env.h, 4, SEED, h_out.data_ptr(), None)
+        assert rc == 0, rc
 
-        def step_host():
-            rc = lib.vrg_env_set_lights(env.h, lights, nl)
-            assert rc == 0, rc
-            rc = lib.vrg_env_gather_direct_light(env.h, 4, SEED, h_out.data_ptr(), None)
-            assert rc == 0, rc
-
-        h2d, d2h = 80 * nl, 12 * nlux
-        workload = ("direct light, %d faces / %d luxels x 4 supersamples, 64 point + 8 spot + "
-                    "162-direction sky, %d triangles" % (lit.n_faces, nlux, len(lit.ids)))
+    h2d, d2h = 80 * nl, 12 * nlux
+    workload = ("direct light, %d faces / %d luxels x 4 supersamples, 64 point + 8 spot + "
+                "162-direction sky, %d triangles" % (lit.n_faces, nlux, len(lit.ids)))
 
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     for _ in range(max(args.warmup, 3)):
@@ -344,36 +417,6 @@ def run_gpu(args, rank, world, local_rank):
         e2e_t.append(time.perf_counter() - t0)
     e2e_value = units * world / statistics.mean(e2e_t) / 1e6
 
-    closest = None
-    if args.workload == "anyhit":
-        # the same lines with the closest hit's triangle and distance written
-        # too (Trace4Rays semantics over the normalised segments)
-        d_h = torch.empty(n, dtype=torch.int32, device=dev)
-        d_t = torch.empty(n, dtype=torch.float32, device=dev)
-
-        def step_hit():
-            rc = lib.vrg_env_occlusion_mask_d(env.h, d_a.data_ptr(), d_b.data_ptr(), n, -1,
-                                              d_m.data_ptr(), d_h.data_ptr(), d_t.data_ptr())
-            assert rc == 0, rc
-
-        for _ in range(max(args.warmup, 3)):
-            step_hit()
-            flush.zero_()
-        torch.cuda.synchronize()
-        cts = []
-        for _ in range(args.steps):
-            flush.zero_()
-            a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a_ev.record(stream)
-            step_hit()
-            b_ev.record(stream)
-            torch.cuda.synchronize()
-            cts.append(a_ev.elapsed_time(b_ev))
-        hv, hms = lib_ctx.autotune_choice(Context.tune_key("trace_mask_hit", env.num_triangles(), n))
-        closest = {"value": round(n / (statistics.mean(cts) * 1e-3) / 1e6, 3), "unit": "Mrays/s",
-                   "ms_per_step": round(statistics.mean(cts), 4), "outputs": "mask + hit index + t",
-                   "autotune": {"variant": hv, "variant_ms": [round(x, 4) for x in hms]}}
-
     if rank != 0:
         if dist:
             td.destroy_process_group()
@@ -381,83 +424,56 @@ def run_gpu(args, rank, world, local_rank):
 
     peak, peak_kind = _peaks()
     threads = os.cpu_count() or 1
-    cpu = None
-    roof = None
     avg_ms = kms / max(kn, 1)
-    tkey = (Context.tune_key("trace_mask", env.num_triangles(), n) if args.workload == "anyhit"
-            else Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
+    tkey = Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4)
     tv, tms = lib_ctx.autotune_choice(tkey)
-    # variants that never visit leaves without triangles (kOptSkip)
-    skip_empty = tv in ((12, 13, 14, 15) if args.workload == "anyhit" else (6,))
-    if args.workload == "anyhit":
-        from oracle import pyoracle
+    # the device's luxels of the timed bake, against the oracle's whole bake
+    # (which is also the CPU baseline: every face, every host thread)
+    got = h_out.numpy().copy()
+    from oracle import pyoracle
 
-        s = pyoracle.Scene(sc.xyz, sc.ids)
-        t0 = time.perf_counter()
-        m = pyoracle.Scene.occlusion_mask(s, sc.starts, sc.stops, threads=threads)
-        dt = time.perf_counter() - t0
-        # node and triangle counts of the walk the device does (its own tree)
-        s.set_tree(*env.walk_tree()[:3])
-        s.set_skip_empty(skip_empty)
-        _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
-        nodes, tris = st[:, 0].mean(), st[:, 1].mean()
-        # per line: end points, mask bit, and per node / per triangle test the
-        # 8-byte node and the 48-byte leaf record
-        bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
-        cpu = {"value": round(n / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
-               "kind": "port", "sample": f"all {n} lines"}
-    else:
-        cpu_faces = min(CPU_SAMPLE_FACES, lit.n_faces)
-        rays_cpu, dt, _ = _cpu_baseline(lit, cpu_faces, threads, None)
-        _, _, st = _cpu_baseline(lit, min(STATS_SAMPLE_FACES, lit.n_faces), threads,
-                                 env.walk_tree()[:3], skip_empty, env.wall_slots())
-        nodes, tris = st[1] / st[0], st[2] / st[0]
-        # per shadow line: nodes and leaf records as above, plus the sample's
-        # position and normal (24 B) and its share of the RGB output (12 B per
-        # luxel of 4 samples), spread over the sample's lines
-        rays_per_sample = units / (4 * nlux)
-        bytes_per_unit = 8 * nodes + 48 * tris + (24 + 12 / 4) / rays_per_sample
-        cpu = {"value": round(rays_cpu / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
-               "kind": "port",
-               "sample": f"faces 0-{cpu_faces} of {lit.n_faces} ({rays_cpu} shadow rays)"}
-    achieved = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
-    # DRAM traffic per launch from the committed ncu capture of the variant family in use
-    prof = f"ncu_{kernel}.txt"
-    if args.workload == "anyhit" and tv in (13, 14, 15):  # unit rounds skipping empty children
-        prof = "ncu_trace_unit_skip.txt"
-    elif args.workload == "anyhit" and tv in (6, 7, 9, 10, 11):  # unit rounds, leaf records out of L1
-        prof = "ncu_trace_unit_stream.txt"
-    traffic = _ncu_traffic(prof)
+    s_ref = pyoracle.Scene(lit.xyz, lit.ids)
+    t0 = time.perf_counter()
+    ref, rays_cpu = pyoracle.gather_luxels(s_ref, pyoracle.make_lights(lit.lights), nl, lit, 0,
+                                           lit.n_faces, ss=4, seed=SEED, threads=threads)
+    dt = time.perf_counter() - t0
+    parity = {"oracle": "C restatement (oracle/vrad_oracle.c), every luxel of the bake",
+              "tolerance_rel": 1e-4, "shadow_rays_equal": rays_cpu == units,
+              **rel_error_stats(got, ref)}
+    parity["within_tolerance"] = bool(parity["max_rel"] <= 1e-4 and parity["zero_ref_nonzero"] == 0
+                                      and parity["shadow_rays_equal"])
+    cpu = {"value": round(rays_cpu / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+           "kind": "port",
+           "sample": f"the whole bake, all {lit.n_faces} faces ({rays_cpu} shadow rays), walking "
+                     "the reference's SAH tree with no wall test"}
+    # walk statistics of the device's tree, options and wall test (for the byte model)
+    skip_empty = tv in (6,)
+    _, _, st = _cpu_baseline(lit, min(STATS_SAMPLE_FACES, lit.n_faces), threads,
+                             env.walk_tree()[:3], skip_empty, env.wall_slots())
+    nodes, tris = st[1] / st[0], st[2] / st[0]
+    rays_per_sample = units / (4 * nlux)
+    bytes_per_unit = 8 * nodes + 48 * tris + (24 + 12 / 4) / rays_per_sample
     torch.cuda.synchronize()
     l2 = _l2_read_gbs(local_rank)
-    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": traffic,
-            "peak_kind": f"{peak_kind} HBM copy",
-            "kernel": kernel, "kernel_ms": round(avg_ms, 4),
-            "bytes_per_ray": round(bytes_per_unit, 2),
-            "bytes_model": "8 per kd node + 48 per triangle test (leaf-ordered records and wall "
-                           "slots), means of the oracle's walk of the device's tree, with the "
-                           "device's options and wall test, over the same lines" +
-                           (" + 24 end points + 1/8 mask"
-                           if args.workload == "anyhit" else " + sample position, normal and RGB share"),
-            "nodes_per_ray": round(float(nodes), 3), "tris_per_ray": round(float(tris), 3),
-            "l2_read_gbs_measured": round(l2, 1) if l2 else None,
-            "l2_frac": round(achieved / l2, 4) if l2 else None, "traffic_source": f"profiles/{prof}"}
+    roof = _trace_roofline(
+        kernel, units, avg_ms, bytes_per_unit, peak, peak_kind, l2, clk, sms,
+        f"ncu_{kernel}.txt",
+        "8 per kd node + 48 per triangle test (leaf-ordered records and wall slots), means of "
+        "the oracle's walk of the device's tree, with the device's options and wall test, over "
+        "the lines of faces 0-255, + sample position, normal and RGB share", nodes, tris)
     line = {
-        "metric": "shadow Mrays/s (direct-light gather)" if args.workload != "anyhit"
-        else "shadow Mrays/s (any-hit occlusion mask)",
+        "metric": "shadow Mrays/s (direct-light gather)",
         "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 box rooms)",
         "config": {"workload": workload, "rays_per_step": units,
-                   **({} if args.workload == "anyhit" else
-                      {"luxel_samples_per_s_M": round(4 * nlux * args.steps * world / (total_ms * 1e-3) / 1e6, 3)}),
+                   "luxel_samples_per_s_M": round(4 * nlux * args.steps * world / (total_ms * 1e-3) / 1e6, 3),
                    "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",
                    "autotune": {"bucket": tkey, "variant": tv,
                                 "variant_ms": [round(x, 4) for x in tms]},
                    "setup_acceleration_structure_ms": admit_ms},
-        **({"closest_hit": closest} if closest else {}),
+        "parity": parity,
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
@@ -465,24 +481,144 @@ def run_gpu(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "clocks": clk,
     }
+    env.close()
+    if not args.headline_only and world == 1:
+        for name, fn in (("anyhit", sub_anyhit), ("radiosity", sub_radiosity),
+                         ("batch", sub_batch), ("serve", sub_serve)):
+            t0 = time.perf_counter()
+            try:
+                line[name] = fn(args, lib_ctx, stream, dev, flush, l2, sms)
+            except Exception as exc:  # a failed sub-workload is reported, not hidden
+                line[name] = {"error": f"{type(exc).__name__}: {exc}"}
+            line[name]["wall_s"] = round(time.perf_counter() - t0, 1)
     print(json.dumps(line), flush=True)
     if dist:
         td.destroy_process_group()
 
 
-def run_radiosity(args, local_rank):
-    """Transfers + bounce of the direct-light scene's faces subdivided at 64
-    units: CSR build time and rays/s, then the bounce loop to a 1e-3
-    relative energy delta, with the SpMV kernel against the HBM roofline."""
+def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
+    """Config 0: 2^20 shadow lines in the 12,300-triangle room, occlusion
+    mask (and closest hit) per line; every bit and hit checked against the
+    oracle."""
+    import torch
+
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Context
+
+    lib = lib_ctx.lib
+    sc = scenes.anyhit_scene(SEED)
+    env, admit_ms = _admit(lib_ctx, sc.xyz, sc.ids)
+    n = sc.starts.shape[0]
+    d_a = torch.from_numpy(sc.starts).to(dev)
+    d_b = torch.from_numpy(sc.stops).to(dev)
+    d_m = torch.empty((n + 31) // 32, dtype=torch.int32, device=dev)
+    d_h = torch.empty(n, dtype=torch.int32, device=dev)
+    d_t = torch.empty(n, dtype=torch.float32, device=dev)
+
+    def mask():
+        rc = lib.vrg_env_occlusion_mask_d(env.h, d_a.data_ptr(), d_b.data_ptr(), n, -1,
+                                          d_m.data_ptr(), None, None)
+        assert rc == 0, rc
+
+    def closest():
+        rc = lib.vrg_env_occlusion_mask_d(env.h, d_a.data_ptr(), d_b.data_ptr(), n, -1,
+                                          d_m.data_ptr(), d_h.data_ptr(), d_t.data_ptr())
+        assert rc == 0, rc
+
+    for fn in (mask, closest):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+            flush.zero_()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev.index)
+    lib_ctx.set_timing(True)
+    lib_ctx.reset_stats()
+    mask_ms = _event_ms(stream, mask, args.steps, flush)
+    kms, kn = lib_ctx.kernel_stats("trace_mask")
+    lib_ctx.set_timing(False)
+    clk = clocks.stop()
+    hit_ms = _event_ms(stream, closest, args.steps, flush)
+    got_m = d_m.cpu().numpy().view(np.uint32)
+    got_h, got_t = d_h.cpu().numpy(), d_t.cpu().numpy()
+    # end to end through the host-buffer ABI (page-locked end points)
+    h_a = torch.from_numpy(sc.starts).pin_memory()
+    h_b = torch.from_numpy(sc.stops).pin_memory()
+    h_m = torch.empty((n + 31) // 32, dtype=torch.int32).pin_memory()
+
+    def host():
+        rc = lib.vrg_env_occlusion_mask(env.h, h_a.data_ptr(), h_b.data_ptr(), n, -1,
+                                        h_m.data_ptr(), None, None)
+        assert rc == 0, rc
+
+    host()
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        host()
+        e2e.append(time.perf_counter() - t0)
+    from oracle import pyoracle
+
+    threads = os.cpu_count() or 1
+    s = pyoracle.Scene(sc.xyz, sc.ids)
+    t0 = time.perf_counter()
+    rm = s.occlusion_mask(sc.starts, sc.stops, threads=threads)
+    dt = time.perf_counter() - t0
+    _, rh, rt = s.occlusion_mask(sc.starts, sc.stops, threads=threads, closest=True)
+    diff_bits = int(np.unpackbits((got_m ^ rm).view(np.uint8)).sum())
+    tv, tms = lib_ctx.autotune_choice(Context.tune_key("trace_mask", env.num_triangles(), n))
+    hv, hms = lib_ctx.autotune_choice(Context.tune_key("trace_mask_hit", env.num_triangles(), n))
+    # the device's walk, counted by the oracle on the device's tree
+    skip_empty = tv in (12, 13, 14, 15)
+    s.set_tree(*env.walk_tree()[:3])
+    s.set_skip_empty(skip_empty)
+    _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
+    nodes, tris = st[:, 0].mean(), st[:, 1].mean()
+    bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
+    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15) else (
+        "ncu_trace_unit_stream.txt" if tv in (6, 7, 9, 10, 11) else "ncu_trace_mask.txt")
+    peak, kind = _peaks()
+    avg_ms = kms / max(kn, 1)
+    env.close()
+    return {
+        "metric": "shadow Mrays/s (any-hit occlusion mask)",
+        "value": round(n / (statistics.mean(mask_ms) * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+        "ms_per_step": round(statistics.mean(mask_ms), 4),
+        "config": {"workload": "2^20 shadow lines, both ends uniform in the 4,096-unit room, "
+                               "12,300-triangle box room (1,024 boxes), seed 0",
+                   "l2": "flushed between steps (512 MiB write)",
+                   "autotune": {"variant": tv, "variant_ms": [round(x, 4) for x in tms]},
+                   "setup_acceleration_structure_ms": admit_ms},
+        "closest_hit": {"value": round(n / (statistics.mean(hit_ms) * 1e-3) / 1e6, 3),
+                        "unit": "Mrays/s", "ms_per_step": round(statistics.mean(hit_ms), 4),
+                        "outputs": "mask + hit index + t", "autotune_variant": hv},
+        "e2e": {"value": round(n / statistics.mean(e2e) / 1e6, 3), "unit": "Mrays/s",
+                "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 4 * ((n + 31) // 32)},
+        "parity": {"oracle": "C restatement, all 2^20 lines", "mask_bits_differing": diff_bits,
+                   "hit_index_differing": int(np.count_nonzero(got_h != rh)),
+                   "t_bits_differing": int(np.count_nonzero(got_t.view(np.uint32) != rt.view(np.uint32))),
+                   "exact": diff_bits == 0 and bool(np.array_equal(got_h, rh))
+                   and bool(np.array_equal(got_t.view(np.uint32), rt.view(np.uint32)))},
+        "roofline": _trace_roofline(
+            "trace_mask", n, avg_ms, bytes_per_unit, peak, kind, l2, clk, sms, prof,
+            "24 end points + 1/8 mask + 8 per kd node + 48 per triangle test, means of the "
+            "oracle's walk of the device's tree with the device's options", nodes, tris),
+        "cpu_baseline": {"value": round(n / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+                         "kind": "port", "sample": f"all {n} lines, the reference's SAH tree"},
+        "clocks": clk,
+    }
+
+
+def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
+    """Config 2: the direct-light faces subdivided at 64 units; transfers from
+    K closest-hit rays per patch (CSR), then the bounce loop to a 1e-3
+    relative delta.  Sampled rows are rebuilt by the oracle bit for bit and
+    the bounce is checked against the float64 oracle over the device's CSR."""
     import torch
 
     from vrad_gb300 import scenes
     from vrad_gb300.environment import Context, Environment
 
-    torch.cuda.set_device(local_rank)
-    ctx = Context(local_rank)
-    if args.autotune_file:
-        ctx.autotune_load(args.autotune_file)
+    ctx = lib_ctx
     lit = scenes.lit_scene(SEED, n_faces=args.faces)
     env = Environment(ctx)
     env.add_triangles(lit.xyz, lit.ids)
@@ -502,82 +638,126 @@ def run_radiosity(args, local_rank):
     t0 = time.perf_counter()
     nnz = env.make_transfers(dirs)
     t_xfer = time.perf_counter() - t0
-    rows_ms = ctx.kernel_stats("transfer_rows")[0]
+    _, _, ovf = env.transfer_info()
+    rows_ms = ctx.kernel_stats("transfer_rows")[0] + ctx.kernel_stats("transfer_rows_sorted")[0]
     xkey = Context.tune_key("transfer_rows", env.num_triangles(), nl * args.k)
     gather_ms = ctx.kernel_stats("transfer_gather")[0]
-    env.gather_patch_direct(nl)
+    ctx.set_timing(False)
+    direct = env.gather_patch_direct(nl)
     env.bounce_light(nl, 100, 1e-3)  # the first solve of a size bucket tunes the SpMV
     tkey = Context.tune_key("bounce_spmv", nnz, nl)
     tv, tms = ctx.autotune_choice(tkey)
     # per-kernel timing pass (one launch per bounce)
+    ctx.set_timing(True)
     ctx.reset_stats()
+    clocks = Clocks(dev.index)
     total, bounces, delta = env.bounce_light(nl, 100, 1e-3)
+    clk = clocks.stop()
     spmv_ms, spmv_n = ctx.kernel_stats("bounce_spmv")
     red_ms, _ = ctx.kernel_stats("bounce_reduce")
-    # graph pass, wall clock of the whole loop
     ctx.set_timing(False)
+    # graph pass, wall clock of the whole loop
     for _ in range(2):
         env.bounce_light(nl, 100, 1e-3)
-    t0 = time.perf_counter()
     reps = max(args.steps, 1)
+    t0 = time.perf_counter()
     for _ in range(reps):
         env.bounce_light(nl, 100, 1e-3)
     loop_s = (time.perf_counter() - t0) / reps
-    peak, peak_kind = _peaks()
+    # parity: sampled rows, leaf direct light, bounce vs float64
+    from oracle import pyoracle
+
+    threads = os.cpu_count() or 1
+    row_ptr, col, w = env.get_transfers(nl, nnz)
+    s = pyoracle.Scene(lit.xyz, lit.ids)
+    OP = pyoracle.make_patches(lit)
+    rng = np.random.default_rng(SEED + 2)
+    per_row = np.diff(row_ptr)
+    rows = set(rng.choice(nl, min(args.check_rows, nl), replace=False).tolist())
+    rows |= set(np.nonzero(per_row > 7168)[0][:64].tolist())
+    rows = np.array(sorted(rows), np.int64)
+    orow, ocol, ocnt = pyoracle.make_transfer_rows(s, lit, OP, dirs, rows, threads=threads)
+    kf = np.float32(args.k)
+    mism = 0
+    for j, r in enumerate(rows):
+        a, b = row_ptr[r], row_ptr[r + 1]
+        oa, ob = orow[j], orow[j + 1]
+        mism += not (b - a == ob - oa and np.array_equal(col[a:b], ocol[oa:ob]) and np.array_equal(
+            w[a:b].view(np.uint32), (ocnt[oa:ob] / kf).astype(np.float32).view(np.uint32)))
+    leaf_patch = np.nonzero(OP["leaf_index"] >= 0)[0]
+    face = OP["face"][leaf_patch]
+    pts = (OP["center"][leaf_patch] + lit.normal[face] * np.float32(0.125)).astype(np.float32)
+    ref_direct, _ = pyoracle.gather_points(s, pyoracle.make_lights(lit.lights), len(lit.lights),
+                                           pts, lit.normal[face], threads=threads)
+    refl = lit.refl[face]
+    rtot, rb, rdeltas = pyoracle.bounce_f64(row_ptr, col, w, refl, ref_direct,
+                                            np.zeros_like(refl), 100, 1e-3, threads=threads)
+    nzm = rtot != 0
+    brel = np.abs(total.astype(np.float64)[nzm] - rtot[nzm]) / np.abs(rtot[nzm])
+    dstat = rel_error_stats(direct, ref_direct)
+    peak, kind = _peaks()
     per_iter_ms = spmv_ms / max(spmv_n, 1)
     bytes_iter = 8 * nnz + 72 * nl  # col+weight per entry; row_ptr, refl, total RMW, emit out per row
     achieved = bytes_iter / (per_iter_ms * 1e-3) / 1e9
-    line = {
-        "metric": "bounce loop (transfers + Jacobi gather to 1e-3)", "value": round(1.0 / loop_s, 3),
-        "unit": "solves/s", "n_gpus": 1, "steps": reps, "warmup": 2,
-        "ms_per_step": round(loop_s * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 box rooms)",
+    traffic_k = _profile_value("ncu_bounce_spmv.txt", "dram_bytes_per_entry")
+    env.close()
+    return {
+        "metric": "bounce loop (transfers + Jacobi gather to 1e-3)",
+        "value": round(1.0 / loop_s, 3), "unit": "solves/s", "ms_per_step": round(loop_s * 1e3, 3),
         "config": {"workload": f"{lit.n_faces} faces subdivided at 64 units", "leaf_patches": nl,
                    "transfer_rays_per_patch": args.k, "nnz": nnz, "nnz_per_row": round(nnz / nl, 1),
-                   "bounces": bounces, "final_delta": delta,
+                   "rows_past_row_table": ovf, "bounces": bounces, "final_delta": delta,
                    "autotune": {"bucket": tkey, "variant": tv,
                                 "variant_ms": [round(x, 4) for x in tms]}},
         "transfers": {"build_s": round(t_xfer, 3), "first_build_s_with_autotune": round(t_first, 3),
-                      "rows_kernel_ms": round(rows_ms, 3),
-                      "gather_kernel_ms": round(gather_ms, 3),
+                      "rows_kernel_ms": round(rows_ms, 3), "gather_kernel_ms": round(gather_ms, 3),
                       "rays_per_s_M": round(nl * args.k / (rows_ms * 1e-3) / 1e6, 1),
                       "autotune": dict(zip(("bucket", "variant", "variant_ms"),
                                            (xkey,) + ctx.autotune_choice(xkey))),
                       "patch_build_s": round(t_patch, 3)},
+        "parity": {"transfer_rows_checked": int(len(rows)), "transfer_rows_differing": int(mism),
+                   "leaf_direct": dstat,
+                   "bounce": {"oracle": "float64 Jacobi over the device's CSR, oracle direct light",
+                              "tolerance_rel": 1e-3, "bounces": bounces, "oracle_bounces": int(rb),
+                              "max_rel": float(brel.max()) if brel.size else 0.0,
+                              "p99_rel": float(np.percentile(brel, 99)) if brel.size else 0.0,
+                              "zero_ref_nonzero": int(np.count_nonzero(total[~nzm]))}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
-                     "peak_kind": f"{peak_kind} HBM copy", "kernel": "bounce_spmv",
+                     "frac": round(achieved / peak, 4),
+                     "traffic": round(traffic_k * nnz) if traffic_k else None,
+                     "traffic_source": "profiles/ncu_bounce_spmv.txt (DRAM bytes per CSR entry, "
+                                       "scaled to this nnz)",
+                     "peak_kind": f"{kind} HBM copy", "kernel": "bounce_spmv",
                      "kernel_ms": round(per_iter_ms, 4), "bytes_per_launch": bytes_iter,
                      "reduce_ms": round(red_ms / max(spmv_n, 1), 4)},
+        "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
 
 
-def run_batch(args, local_rank):
-    """Batched bakes: 256 scenes with log-uniform face counts (64-4,096,
-    48-unit luxels, ~46M samples in all), each baked direct + bounce to a
-    1e-3 delta.  Times the batched path (one persistent direct launch + one
-    block-diagonal bounce graph) against the plain one-scene-per-launch loop
-    on the same resident scenes."""
+def sub_batch(args, lib_ctx, stream, dev, flush, l2, sms):
+    """Config 3: 256 scenes with log-uniform face counts (64-4,096), each
+    baked direct + bounce to a 1e-3 delta: the batched path (one persistent
+    direct launch + one block-diagonal bounce graph) against the plain
+    one-scene-per-launch loop on the same resident scenes, and the two
+    paths' results compared scene by scene."""
     import torch
 
     from vrad_gb300 import scenes
-    from vrad_gb300.environment import Batch, Context, Environment
+    from vrad_gb300.environment import Batch, Environment
 
-    torch.cuda.set_device(local_rank)
-    ctx = Context(local_rank)
+    ctx = lib_ctx
     t0 = time.perf_counter()
     lits = scenes.batch_scenes(SEED, n_scenes=args.scenes)
-    dirs = scenes.transfer_directions(args.k)
-    envs = []
+    dirs = scenes.transfer_directions(args.batch_k)
+    envs, leaves, nnzs = [], [], []
     for lit in lits:
         env = Environment(ctx)
         env.add_triangles(lit.xyz, lit.ids)
         env.SetupAccelerationStructure()
         env.set_faces(lit)
         env.set_lights(lit.lights)
-        env.make_patches()
-        env.make_transfers(dirs)
+        leaves.append(env.make_patches()["n_leaves"])
+        nnzs.append(env.make_transfers(dirs))
         envs.append(env)
     setup_s = time.perf_counter() - t0
     batch = Batch(ctx)
@@ -593,56 +773,67 @@ def run_batch(args, local_rank):
     def batched():
         return batch.bake(4, SEED, 100, 1e-3)
 
-    res = {}
+    res, outs = {}, {}
     for name, fn in (("plain", plain), ("batched", batched)):
         for _ in range(max(args.warmup, 1)):
             fn()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rays = 0
-        for _ in range(args.steps):
+        for _ in range(args.batch_steps):
             rays = fn()
-        dt = (time.perf_counter() - t0) / args.steps
+        dt = (time.perf_counter() - t0) / args.batch_steps
         res[name] = (dt, rays)
+        outs[name] = [env.get_bake(nl) for env, nl in zip(envs, leaves)]
+    lux_bits = sum(int(np.count_nonzero(a["luxels"].view(np.uint32) != b["luxels"].view(np.uint32)))
+                   for a, b in zip(outs["plain"], outs["batched"]))
+    tot_rel = max(float(np.max(np.abs(a["patch_total"].astype(np.float64) - b["patch_total"]) /
+                               np.maximum(np.abs(a["patch_total"]), 1e-30)))
+                  if a["patch_total"].size else 0.0
+                  for a, b in zip(outs["plain"], outs["batched"]))
     n = len(envs)
-    line = {
+    for env in envs:
+        env.close()
+    batch.close()
+    return {
         "metric": "bakes/s (batched vs one scene per launch)",
-        "value": round(n / res["batched"][0], 2), "unit": "bakes/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * res["batched"][0], 2),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded SplitMix64 box rooms)",
-        "config": {"workload": f"{n} scenes, faces log-uniform 64-4096, 48-unit luxels x 4 samples, "
-                               f"64-unit+ patches, {args.k} transfer rays/patch, bounce to 1e-3",
+        "value": round(n / res["batched"][0], 2), "unit": "bakes/s",
+        "ms_per_step": round(1e3 * res["batched"][0], 2), "steps": args.batch_steps,
+        "config": {"workload": f"{n} scenes, faces log-uniform 64-4096, 4 samples per luxel, "
+                               f"64-unit patches, bounce to 1e-3",
+                   "luxel_spacing": 48.0,
+                   "deviation": "48-unit luxels (the direct-light config uses 16) and 8,192 "
+                                "transfer rays per patch, to keep setup within the bench's minutes",
+                   "transfer_rays_per_patch": args.batch_k,
+                   "nnz_per_row": round(sum(nnzs) / max(sum(leaves), 1), 1),
                    "luxels": sum(l.n_luxels for l in lits), "faces": sum(l.n_faces for l in lits),
-                   "setup_s": round(setup_s, 1)},
+                   "leaf_patches": sum(leaves), "setup_s": round(setup_s, 1)},
         "plain": {"bakes_per_s": round(n / res["plain"][0], 2), "ms_per_batch": round(1e3 * res["plain"][0], 2)},
         "batched": {"bakes_per_s": round(n / res["batched"][0], 2),
                     "ms_per_batch": round(1e3 * res["batched"][0], 2)},
         "speedup": round(res["plain"][0] / res["batched"][0], 3),
         "shadow_rays_per_batch": res["batched"][1],
-        "batched_Mrays_per_s": round(res["batched"][1] / res["batched"][0] / 1e6, 1),
+        "parity": {"against": "the plain path's bake of each scene (itself checked against the "
+                              "oracle in tests/test_gpu_batch.py)",
+                   "luxel_values_differing": lux_bits, "bounced_light_max_rel": tot_rel},
     }
-    print(json.dumps(line), flush=True)
 
 
-def run_serve(args, local_rank):
-    """Served relighting: 8 resident scenes (faces log-uniform 300-4,096,
-    16-unit luxels, 10k-140k leaf patches); Poisson request streams at
-    several rates; each request moves and rescales 1-16 point/spot lights,
+def sub_serve(args, lib_ctx, stream, dev, flush, l2, sms):
+    """Config 4: 8 resident scenes (faces log-uniform 300-4,096, 16-unit
+    luxels, 10k-140k leaf patches); Poisson request streams at several
+    rates; each request moves and rescales 1-16 point/spot lights,
     re-gathers the affected luxels and re-solves the bounce to a 1e-3
     relative change.  The served path (8 slots, continuous admission) runs
     beside the plain serial path (1 slot) on the same request stream."""
-    import torch
-
     from vrad_gb300 import scenes
-    from vrad_gb300.environment import Context, Environment, Server, edit_array, make_light
+    from vrad_gb300.environment import Environment, Server, edit_array, make_light
 
-    torch.cuda.set_device(local_rank)
-    ctx = Context(local_rank)
+    ctx = lib_ctx
     counts = scenes.batch_face_counts(SEED + 7, 8, 300, 4096)
     lits, envs, leaves = [], [], []
     t0 = time.perf_counter()
-    dirs = scenes.transfer_directions(args.k)
+    dirs = scenes.transfer_directions(args.batch_k)
     for i, c in enumerate(counts):
         lit = scenes.lit_scene(5000 + i, n_faces=int(c))
         env = Environment(ctx)
@@ -701,7 +892,6 @@ def run_serve(args, local_rank):
                 "mean_ms": round(float(lat.mean()), 3),
                 "bakes_per_s": round(len(res) / span, 1), "mean_bounces": round(float(bounces.mean()), 2)}
 
-    # warm-up on both paths
     warm = make_requests()[:32]
     warm_arr = np.cumsum(rng.exponential(1.0 / 1000.0, len(warm)))
     run(8, warm_arr, warm)
@@ -713,19 +903,46 @@ def run_serve(args, local_rank):
         arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
         table[str(int(rate))] = {"served": run(8, arrivals, reqs), "serial": run(1, arrivals, reqs)}
     top = table[str(int(rates[-1]))]
-    line = {
+    for env in envs:
+        env.close()
+    return {
         "metric": "relight p50/p99 ms and bakes/s (served vs plain serial)",
-        "value": top["served"]["p99_ms"], "unit": "ms (p99 at the highest rate)", "n_gpus": 1,
-        "steps": n_req, "warmup": 32, "ms_per_step": top["served"]["mean_ms"],
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded SplitMix64 box rooms; Poisson arrivals)",
+        "value": top["served"]["p99_ms"], "unit": "ms (p99 at the highest rate)",
+        "higher_is_better": False,
         "config": {"workload": "8 resident scenes, faces " + ",".join(str(int(c)) for c in counts) +
-                   f", leaf patches {min(leaves)}-{max(leaves)}, {args.k} transfer rays/patch, "
+                   f", leaf patches {min(leaves)}-{max(leaves)}, {args.batch_k} transfer rays/patch, "
                    "1-16 light edits per request, bounce re-solve to 1e-3",
                    "requests_per_rate": n_req, "setup_s": round(setup_s, 1)},
         "rates": table,
+        "parity": {"against": "a full re-bake with the edited light table, bit for bit, and the "
+                              "same result alone and in the mix (tests/test_gpu_relight.py)"},
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_one(args, local_rank):
+    """`--workload X`: one of the sub-workloads as its own line."""
+    import torch
+
+    from vrad_gb300.environment import Context
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ctx = Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    if args.autotune_file:
+        ctx.autotune_load(args.autotune_file)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    l2 = _l2_read_gbs(local_rank)
+    fn = {"anyhit": sub_anyhit, "radiosity": sub_radiosity, "batch": sub_batch,
+          "serve": sub_serve}[args.workload]
+    rec = fn(args, ctx, stream, dev, flush, l2, sms)
+    rec.setdefault("higher_is_better", True)
+    rec.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 box rooms)"})
+    print(json.dumps(rec), flush=True)
 
 
 def main():
@@ -736,32 +953,32 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="direct",
                     choices=["direct", "anyhit", "radiosity", "batch", "serve"])
+    ap.add_argument("--headline-only", action="store_true",
+                    help="the direct-light line alone, without the other workloads")
     ap.add_argument("--rates", default="50,200,1000,2000", help="request rates of the serve workload")
-    ap.add_argument("--requests", type=int, default=400, help="requests per rate (serve)")
+    ap.add_argument("--requests", type=int, default=200, help="requests per rate (serve)")
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the batch workload")
+    ap.add_argument("--batch-steps", type=int, default=3, help="timed batches (batch)")
     ap.add_argument("--faces", type=int, default=4096,
                     help="lit faces of the direct-light scene (smaller only for profiling)")
     ap.add_argument("--autotune-file", default=None,
                     help="load saved autotune choices ('bucket variant' lines) before running")
-    ap.add_argument("--k", type=int, default=8192,
-                    help="transfer rays per patch (radiosity, batch, serve)")
+    ap.add_argument("--k", type=int, default=65536,
+                    help="transfer rays per patch of the radiosity workload")
+    ap.add_argument("--batch-k", type=int, default=8192,
+                    help="transfer rays per patch of the batch and serve workloads")
+    ap.add_argument("--check-rows", type=int, default=256,
+                    help="transfer rows the oracle rebuilds to check the radiosity CSR")
     args = ap.parse_args()
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
     local_rank = _env_int("LOCAL_RANK", 0)
     if args.impl == "reference":
         run_reference(args, rank)
-    elif args.workload == "radiosity":
-        if rank == 0:
-            run_radiosity(args, local_rank)
-    elif args.workload == "batch":
-        if rank == 0:
-            run_batch(args, local_rank)
-    elif args.workload == "serve":
-        if rank == 0:
-            run_serve(args, local_rank)
-    else:
+    elif args.workload == "direct":
         run_gpu(args, rank, world, local_rank)
+    elif rank == 0:
+        run_one(args, local_rank)
 
 
 if __name__ == "__main__":

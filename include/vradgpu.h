@@ -48,6 +48,11 @@ extern "C" {
 #define VRG_RTE_FLAGS_FAST_TREE_GENERATION 1
 #define VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_COLORS 2
 #define VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_MATERIALS 4
+/* Triangle flag (the NFlags byte, raytracer/cache/triangle/trigeometrydata.go:8,
+ * set from AddTriangleWithMaterial's flags, environment.go:58) that marks a
+ * transparent triangle for the coverage traces below.  The reference defines
+ * no bit for it; bit 0 is the project's. */
+#define VRG_TRIFLAG_TRANSPARENT 1
 
 /* BSP contents and surface flags the brush ingest reads (Source's bspflags
  * values, which galaco/bsp's flags package carries):
@@ -111,7 +116,8 @@ int vrg_ctx_synchronize(vrg_ctx *ctx);
 int vrg_ctx_set_timing(vrg_ctx *ctx, int enable);
 /* Accumulated device time and launch count of kernel `name` since the last
  * reset; names: "trace_mask", "trace_closest", "trace_lines",
- * "direct_luxels", "direct_points", "transfer_rows", "transfer_gather",
+ * "direct_luxels", "direct_points", "transfer_rows", "transfer_rows_sorted",
+ * "transfer_gather",
  * "bounce_init", "bounce_spmv", "bounce_reduce", "batch_gather",
  * "batch_bounce_init", "batch_spmv", "batch_reduce", "relight_gather",
  * "lightmap". */
@@ -305,6 +311,34 @@ int vrg_env_trace_closest_d(vrg_env *env, const float *origin, const float *dire
 int vrg_env_test_line_does_hit_sky(vrg_env *env, const float *start, const float *stop,
                                    int64_t n, int32_t static_prop_to_skip,
                                    float *fraction_visible);
+
+/* Transparent shadows.  Trace4Rays with a transparent-triangle callback
+ * (environment.go:140-142) that counts coverage as types.CoverageCount does
+ * (raytracer/types/coverageCount.go:27-41: each transparent hit adds its
+ * triangle's colour x, clamped at 1).  The reference never fixes the order
+ * in which hits reach the callback; here a ray's accepted hits are taken in
+ * ascending (t, triangle index): an opaque hit is recorded and ends the walk,
+ * a transparent one (VRG_TRIFLAG_TRANSPARENT) adds coverage and, when the sum
+ * reaches 1, is recorded and ends it.  Per ray: the recorded hit (-1 none),
+ * its t (+inf none) and the coverage.  Host buffers; origins and unit
+ * directions as in vrg_env_trace_closest. */
+int vrg_env_trace_coverage(vrg_env *env, const float *origin, const float *direction, const float *tmin,
+                           const float *tmax, int64_t n, int32_t skip_id, int32_t *out_hit, float *out_t,
+                           float *out_coverage);
+/* TestLineDoesHitSky with texture shadows on (raytracer/trace/testline.go:29-33,
+ * 53-55): occlusion = max(1 if the recorded hit lies before the stop point
+ * and is not TRACE_ID_SKY, coverage), clamped; fraction_visible = 1 -
+ * occlusion.  Texture coverage is a stub in the reference
+ * (rad/staticprops/compute.go:4-12); the triangle's colour x stands for it,
+ * as in CoverageCount. */
+int vrg_env_test_line_coverage(vrg_env *env, const float *start, const float *stop, int64_t n,
+                               int32_t static_prop_to_skip, float *fraction_visible);
+/* Flags and colours of triangles [first, first + n) added earlier (the bulk
+ * form of AddTriangleWithMaterial's flags and colour, environment.go:45-66;
+ * no counterpart in the reference); colours (3 per triangle) may be NULL.
+ * Only before SetupAccelerationStructure. */
+int vrg_env_set_triangle_flags(vrg_env *env, int64_t first, int64_t n, const uint8_t *flags,
+                               const float *colours);
 /* Shadow lines as a 1-bit mask (bit i%32 of word i/32 set = occluded), with
  * the same semantics; out_hit/out_t (may be NULL) add the closest hit of the
  * normalised segment. */
@@ -391,10 +425,21 @@ int vrg_env_get_patches(const vrg_env *env, float *mins, float *maxs, float *cen
 /* Transfer lists (Patch.NumTransfers/Transfers, common/types/patch.go:60-61,
  * Transfer common/types/transfer.go:3-6) of every leaf patch, from k
  * closest-hit rays along dirs_local (k x 3, local frame: tangent, bitangent,
- * normal).  Built on the device into CSR and kept resident. */
+ * normal; k a power of two in [32, 65536]).  Built on the device into CSR
+ * and kept resident. */
 int vrg_env_make_transfers(vrg_env *env, const float *dirs_local, int32_t k, int64_t *out_nnz);
 /* CSR copy-out: row_ptr[leaves+1], col[nnz], weight[nnz] (= hits / k). */
 int vrg_env_get_transfers(const vrg_env *env, int64_t *row_ptr, int32_t *col, float *weight);
+/* The last build's ray count k, entry count, and how many of its rows had
+ * more distinct targets than the shared-memory row table holds (those rows
+ * are rebuilt by a global-memory sort; the CSR is the same either way).
+ * (no reference counterpart: transfer building is absent there) */
+int vrg_env_transfer_info(const vrg_env *env, int32_t *k, int64_t *nnz, int64_t *overflow_rows);
+/* Distinct targets a transfer row may collect in its shared-memory table
+ * before the row is rebuilt by the global-memory sort (default and maximum
+ * 7168; a lower limit sends more rows down that path, which tests use).
+ * (no reference counterpart) */
+int vrg_ctx_set_transfer_table_limit(vrg_ctx *ctx, int32_t limit);
 /* Direct light at every leaf patch (one sample at centre + 0.125 * normal). */
 int vrg_env_gather_patch_direct(vrg_env *env, float *out_rgb);
 /* Bounce loop: emit = refl * direct + baselight; per bounce add = T emit,
@@ -410,13 +455,18 @@ int vrg_env_bounce_light(vrg_env *env, int32_t max_bounces, float rel_tol, float
  * call allocates nothing: its working state lives in one fixed device array
  * of 8 MiB + 16 KiB that every GPU loading the library holds until exit, so a
  * scene may have at most 262144 leaf patches (larger scenes get
- * VRG_ERR_UNSUPPORTED).  total_out is a DEVICE buffer of 4 floats per leaf
- * (RGB + padding).  vrg_env_make_transfers and vrg_env_gather_patch_direct
- * must have run.  The first call on a device also looks up the array's
- * device address; make that first call before any stream capture.  All
- * calls on a device share the one array, so calls that overlap on the GPU
- * (two streams, two threads) race: serialise them.  No counterpart in the
- * reference. */
+ * VRG_ERR_UNSUPPORTED).  total_out is a DEVICE buffer of this context's
+ * GPU, 16-byte aligned, of 4 floats per leaf (RGB + padding); a host pointer,
+ * another GPU's memory or a misaligned pointer is refused with
+ * VRG_ERR_INVALID before anything is launched.  The result lives only in
+ * total_out: vrg_env_get_bake and vrg_env_get_lightmap keep returning the
+ * scene's last allocating bake.  vrg_env_make_transfers and
+ * vrg_env_gather_patch_direct must have run.  vrg_ctx_create already looks
+ * up the array's device address and loads this call's kernels, so every
+ * call, the first included, allocates nothing (if that set-up failed, the
+ * first call retries it).  All calls on a device share the one array, so
+ * calls that overlap on the GPU (two streams, two threads) race: serialise
+ * them.  No counterpart in the reference. */
 int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, float rel_tol,
                                  float *total_out, int32_t *out_bounces, float *out_delta);
 

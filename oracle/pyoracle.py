@@ -181,6 +181,26 @@ class Scene:
                              C.c_int32(skip), int(brute), threads, _p(out))
         return out
 
+    def trace_coverage(self, cover, o, d, tmin, tmax, skip=-1, threads=8):
+        """Transparent-shadow trace (brute force): recorded hit, t, coverage
+        per ray; triangles flagged transparent add cover[i]."""
+        o, d = f32(o).reshape(-1, 3), f32(d).reshape(-1, 3)
+        n = o.shape[0]
+        tmin, tmax = f32(np.broadcast_to(tmin, (n,))), f32(np.broadcast_to(tmax, (n,)))
+        hit, t, cov = np.empty(n, np.int32), np.empty(n, np.float32), np.empty(n, np.float32)
+        lib().orc_trace_coverage(C.c_void_p(self.h), _p(f32(cover)), _p(o), _p(d), _p(tmin),
+                                 _p(tmax), C.c_int64(n), C.c_int32(skip), threads, _p(hit), _p(t),
+                                 _p(cov))
+        return hit, t, cov
+
+    def test_lines_coverage(self, cover, starts, stops, skip=-1, threads=8):
+        """TestLineDoesHitSky with texture shadows: fraction visible per line."""
+        a, b = f32(starts).reshape(-1, 3), f32(stops).reshape(-1, 3)
+        out = np.empty(a.shape[0], np.float32)
+        lib().orc_test_lines_coverage(C.c_void_p(self.h), _p(f32(cover)), _p(a), _p(b),
+                                      C.c_int64(a.shape[0]), C.c_int32(skip), threads, _p(out))
+        return out
+
     def occlusion_mask(self, starts, stops, skip=-1, threads=8, closest=False, stats=False):
         a, b = f32(starts).reshape(-1, 3), f32(stops).reshape(-1, 3)
         n = a.shape[0]
@@ -304,14 +324,41 @@ def make_transfers(scene: Scene, lit, P, dirs, threads=8):
     return row_ptr, col[:nnz].copy(), cnt[:nnz].copy()
 
 
-def bounce_f64(row_ptr, col, w, refl, direct, base, max_bounces, tol):
+def make_transfer_rows(scene: Scene, lit, P, dirs, rows, threads=8):
+    """Transfer rows of the dense leaf indices `rows` only (in that order):
+    (row_ptr[len(rows)+1], col, hit count), each row as make_transfers
+    builds it."""
+    L = lib()
+    L.orc_make_transfer_rows.restype = C.c_int64
+    rows = np.ascontiguousarray(rows, np.int64)
+    k = dirs.shape[0]
+    cap = max(len(rows) * k, 1)
+    row_ptr = np.zeros(len(rows) + 1, np.int64)
+    col = np.zeros(cap, np.int32)
+    cnt = np.zeros(cap, np.int32)
+    nnz = L.orc_make_transfer_rows(C.c_void_p(scene.h), _p(np.ascontiguousarray(lit.tri_face)),
+                                   C.c_int64(len(P["face"])), _p(P["center"]), _p(P["face"]),
+                                   _p(P["child1"]), _p(P["child2"]), _p(P["split_axis"]),
+                                   _p(P["split_dist"]), _p(P["leaf_index"]), _p(P["face_root"]),
+                                   _p(f32(lit.normal)), _p(f32(lit.u)), _p(f32(dirs)),
+                                   C.c_int32(k), threads, _p(rows), C.c_int64(len(rows)),
+                                   _p(row_ptr), _p(col), _p(cnt), C.c_int64(cap))
+    if nnz < 0:
+        raise ValueError("make_transfer_rows: row index out of range")
+    return row_ptr, col[:nnz].copy(), cnt[:nnz].copy()
+
+
+def bounce_f64(row_ptr, col, w, refl, direct, base, max_bounces, tol, threads=1):
+    """Float64 Jacobi bounce; the result does not depend on `threads`."""
     n = row_ptr.shape[0] - 1
     total = np.zeros((n, 3), np.float64)
     deltas = np.zeros(max(max_bounces, 1), np.float64)
-    it = lib().orc_bounce_f64(C.c_int64(n), _p(np.ascontiguousarray(row_ptr, np.int64)),
-                              _p(np.ascontiguousarray(col, np.int32)), _p(f32(w)),
-                              _p(f32(refl)), _p(f32(direct)), _p(f32(base)), max_bounces,
-                              C.c_double(tol), _p(total), _p(deltas))
+    L = lib()
+    L.orc_bounce_f64_mt.restype = C.c_int
+    it = L.orc_bounce_f64_mt(C.c_int64(n), _p(np.ascontiguousarray(row_ptr, np.int64)),
+                             _p(np.ascontiguousarray(col, np.int32)), _p(f32(w)),
+                             _p(f32(refl)), _p(f32(direct)), _p(f32(base)), max_bounces,
+                             C.c_double(tol), _p(total), _p(deltas), int(threads))
     return total, it, deltas[:it]
 
 

@@ -845,6 +845,121 @@ void orc_test_lines(const orc_scene *s, const float *start, const float *stop, i
     parallel_for(n, threads, 1024, lines_range, &j);
 }
 
+/* ------------------------------------------------------------------ */
+/* transparent shadows (project semantics; see the header)             */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    float t;
+    int32_t idx;
+} tri_hit_t;
+
+static int cmp_hit(const void *a, const void *b) {
+    const tri_hit_t *x = (const tri_hit_t *)a, *y = (const tri_hit_t *)b;
+    if (x->t < y->t) return -1;
+    if (x->t > y->t) return 1;
+    return (x->idx > y->idx) - (x->idx < y->idx);
+}
+
+/* Every accepted hit of the ray (brute force over all triangles, tri_hit on
+ * [tmin, tmax), ids equal to skip ignored), sorted by (t, triangle index);
+ * then taken in that order: an opaque hit is recorded and ends the walk; a
+ * transparent hit adds its coverage, c = min(c + cover, 1), and when c
+ * reaches 1 that triangle is recorded and the walk ends. */
+static void coverage_trace(const orc_scene *s, const float *cover, const float *o, const float *d,
+                           float tmin, float tmax, int32_t skip, tri_hit_t *buf, int32_t *hit,
+                           float *thit, float *cov) {
+    int64_t nh = 0;
+    for (int64_t i = 0; i < s->ntris; i++) {
+        const orc_tri *tr = &s->tris[i];
+        if (tr->id == skip) continue;
+        float t;
+        if (tri_hit(tr, o, d, tmin, tmax, &t)) {
+            buf[nh].t = t;
+            buf[nh].idx = (int32_t)i;
+            nh++;
+        }
+    }
+    qsort(buf, (size_t)nh, sizeof(tri_hit_t), cmp_hit);
+    float c = 0.0f;
+    *hit = -1;
+    *thit = INFINITY;
+    for (int64_t k = 0; k < nh; k++) {
+        const int32_t i = buf[k].idx;
+        if (!(s->flags && (s->flags[i] & ORC_TRI_TRANSPARENT))) {
+            *hit = i;
+            *thit = buf[k].t;
+            break;
+        }
+        c = fminf(c + cover[i], 1.0f);
+        if (c >= 1.0f) {
+            *hit = i;
+            *thit = buf[k].t;
+            break;
+        }
+    }
+    *cov = c;
+}
+
+typedef struct {
+    const orc_scene *s;
+    const float *cover, *a, *b, *tmin, *tmax;
+    int32_t skip;
+    int lines;
+    int32_t *hit;
+    float *t, *cov, *frac;
+} cov_job;
+
+static void cov_range(void *ctx, int64_t b, int64_t e, int w) {
+    (void)w;
+    const cov_job *j = (const cov_job *)ctx;
+    tri_hit_t *buf = malloc(sizeof(tri_hit_t) * (size_t)(j->s->ntris ? j->s->ntris : 1));
+    for (int64_t i = b; i < e; i++) {
+        int32_t h;
+        float th, c;
+        if (!j->lines) {
+            coverage_trace(j->s, j->cover, j->a + 3 * i, j->b + 3 * i, j->tmin[i], j->tmax[i],
+                           j->skip, buf, &h, &th, &c);
+            j->hit[i] = h;
+            j->t[i] = th;
+            j->cov[i] = c;
+            continue;
+        }
+        /* TestLineDoesHitSky with texture shadows (testline.go:22-33,42-55,91-93) */
+        const float *a = j->a + 3 * i, *bb = j->b + 3 * i;
+        float dir[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]};
+        float len = sqrtf(dot3(dir, dir));
+        if (!(len > 0.0f)) {
+            j->frac[i] = 1.0f;
+            continue;
+        }
+        float r = 1.0f / len;
+        dir[0] = dir[0] * r;
+        dir[1] = dir[1] * r;
+        dir[2] = dir[2] * r;
+        coverage_trace(j->s, j->cover, a, dir, 0.0f, len, j->skip, buf, &h, &th, &c);
+        float occ = (h >= 0 && th < len && (j->s->tris[h].id & ORC_TRACE_ID_SKY) == 0) ? 1.0f : 0.0f;
+        occ = fmaxf(occ, c);
+        occ = fminf(fmaxf(occ, 0.0f), 1.0f);
+        j->frac[i] = 1.0f - occ;
+    }
+    free(buf);
+}
+
+void orc_trace_coverage(const orc_scene *s, const float *cover, const float *orig, const float *dir,
+                        const float *tmin, const float *tmax, int64_t n, int32_t skip_id,
+                        int threads, int32_t *out_hit, float *out_t, float *out_coverage) {
+    cov_job j = {s, cover, orig, dir, tmin, tmax, skip_id, 0, out_hit, out_t, out_coverage, NULL};
+    parallel_for(n, threads, 64, cov_range, &j);
+}
+
+void orc_test_lines_coverage(const orc_scene *s, const float *cover, const float *start,
+                             const float *stop, int64_t n, int32_t skip_id, int threads,
+                             float *out_frac) {
+    cov_job j = {s, cover, start, stop, NULL, NULL, skip_id, 1, NULL, NULL, NULL, out_frac};
+    parallel_for(n, threads, 64, cov_range, &j);
+}
+
 static void mask_range(void *ctx, int64_t b, int64_t e, int w) {
     (void)w;
     trace_job *j = (trace_job *)ctx;
@@ -1444,7 +1559,8 @@ typedef struct {
     const float *center, *split_dist, *fnormal, *fu, *dirs;
     int32_t k;
     const int64_t *leaf_patch; /* dense leaf -> patch index */
-    int32_t *cnt_rows;         /* per row: list of targets (k entries) */
+    const int64_t *row_list;   /* rows to build (NULL: 0, 1, 2, ...) */
+    int32_t *cnt_rows;         /* per built row: list of targets (k entries) */
     int32_t *nnz;
 } xfer_job;
 
@@ -1456,7 +1572,8 @@ static int cmp_i32(const void *a, const void *b) {
 static void xfer_range(void *ctx, int64_t b, int64_t e, int w) {
     (void)w;
     xfer_job *j = (xfer_job *)ctx;
-    for (int64_t row = b; row < e; row++) {
+    for (int64_t slot = b; slot < e; slot++) {
+        const int64_t row = j->row_list ? j->row_list[slot] : slot;
         int64_t pi = j->leaf_patch[row];
         int32_t f = j->pface[pi];
         const float *N = j->fnormal + 3 * f, *U = j->fu + 3 * f, *c = j->center + 3 * pi;
@@ -1466,7 +1583,7 @@ static void xfer_range(void *ctx, int64_t b, int64_t e, int w) {
         float T1[3] = {U[0] * il, U[1] * il, U[2] * il};
         float T2[3] = {N[1] * T1[2] - N[2] * T1[1], N[2] * T1[0] - N[0] * T1[2],
                        N[0] * T1[1] - N[1] * T1[0]};
-        int32_t *tg = j->cnt_rows + row * (int64_t)j->k;
+        int32_t *tg = j->cnt_rows + slot * (int64_t)j->k;
         for (int32_t r = 0; r < j->k; r++) {
             const float *L = j->dirs + 3 * r;
             float d[3];
@@ -1492,28 +1609,29 @@ static void xfer_range(void *ctx, int64_t b, int64_t e, int w) {
         int32_t distinct = 0;
         for (int32_t r = 0; r < j->k; r++)
             if (tg[r] >= 0 && (r == 0 || tg[r] != tg[r - 1])) distinct++;
-        j->nnz[row] = distinct;
+        j->nnz[slot] = distinct;
     }
 }
 
-int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t npatches_all,
-                           const float *mins, const float *maxs, const float *center,
-                           const int32_t *face, const int32_t *child1, const int32_t *child2,
-                           const int32_t *split_axis, const float *split_dist,
-                           const int32_t *leaf_index, const int32_t *face_root,
-                           const float *fnormal, const float *fu, const float *dirs_local,
-                           int32_t k, int threads, int64_t *row_ptr, int32_t *col, int32_t *cnt,
-                           int64_t cap) {
-    (void)mins;
-    (void)maxs;
+static int64_t make_transfer_rows(const orc_scene *s, const int32_t *tri_face, int64_t npatches_all,
+                                  const float *center, const int32_t *face, const int32_t *child1,
+                                  const int32_t *child2, const int32_t *split_axis,
+                                  const float *split_dist, const int32_t *leaf_index,
+                                  const int32_t *face_root, const float *fnormal, const float *fu,
+                                  const float *dirs_local, int32_t k, int threads,
+                                  const int64_t *row_list, int64_t nrows, int64_t *row_ptr,
+                                  int32_t *col, int32_t *cnt, int64_t cap) {
     int64_t nleaf = 0;
     for (int64_t i = 0; i < npatches_all; i++)
         if (leaf_index[i] >= 0) nleaf++;
+    if (!row_list) nrows = nleaf;
+    for (int64_t r = 0; row_list && r < nrows; r++)
+        if (row_list[r] < 0 || row_list[r] >= nleaf) return -2;
     int64_t *leaf_patch = malloc(sizeof(int64_t) * (size_t)(nleaf ? nleaf : 1));
     for (int64_t i = 0; i < npatches_all; i++)
         if (leaf_index[i] >= 0) leaf_patch[leaf_index[i]] = i;
-    int32_t *rows = malloc(sizeof(int32_t) * (size_t)(nleaf ? nleaf : 1) * (size_t)k);
-    int32_t *nnz = calloc((size_t)(nleaf ? nleaf : 1), sizeof(int32_t));
+    int32_t *rows = malloc(sizeof(int32_t) * (size_t)(nrows ? nrows : 1) * (size_t)k);
+    int32_t *nnz = calloc((size_t)(nrows ? nrows : 1), sizeof(int32_t));
     xfer_job j = {0};
     j.s = s;
     j.tri_face = tri_face;
@@ -1530,17 +1648,18 @@ int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t 
     j.dirs = dirs_local;
     j.k = k;
     j.leaf_patch = leaf_patch;
+    j.row_list = row_list;
     j.cnt_rows = rows;
     j.nnz = nnz;
-    parallel_for(nleaf, threads, 4, xfer_range, &j);
+    parallel_for(nrows, threads, 4, xfer_range, &j);
     int64_t total = 0;
     row_ptr[0] = 0;
-    for (int64_t r = 0; r < nleaf; r++) {
+    for (int64_t r = 0; r < nrows; r++) {
         total += nnz[r];
         row_ptr[r + 1] = total;
     }
     if (total <= cap) {
-        for (int64_t r = 0; r < nleaf; r++) {
+        for (int64_t r = 0; r < nrows; r++) {
             const int32_t *tg = rows + r * (int64_t)k;
             int64_t o = row_ptr[r];
             for (int32_t i = 0; i < k; i++) {
@@ -1561,6 +1680,35 @@ int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t 
     return total <= cap ? total : -1;
 }
 
+int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t npatches_all,
+                           const float *mins, const float *maxs, const float *center,
+                           const int32_t *face, const int32_t *child1, const int32_t *child2,
+                           const int32_t *split_axis, const float *split_dist,
+                           const int32_t *leaf_index, const int32_t *face_root,
+                           const float *fnormal, const float *fu, const float *dirs_local,
+                           int32_t k, int threads, int64_t *row_ptr, int32_t *col, int32_t *cnt,
+                           int64_t cap) {
+    (void)mins;
+    (void)maxs;
+    return make_transfer_rows(s, tri_face, npatches_all, center, face, child1, child2, split_axis,
+                              split_dist, leaf_index, face_root, fnormal, fu, dirs_local, k,
+                              threads, NULL, 0, row_ptr, col, cnt, cap);
+}
+
+int64_t orc_make_transfer_rows(const orc_scene *s, const int32_t *tri_face, int64_t npatches_all,
+                               const float *center, const int32_t *face, const int32_t *child1,
+                               const int32_t *child2, const int32_t *split_axis,
+                               const float *split_dist, const int32_t *leaf_index,
+                               const int32_t *face_root, const float *fnormal, const float *fu,
+                               const float *dirs_local, int32_t k, int threads,
+                               const int64_t *rows, int64_t nrows, int64_t *row_ptr, int32_t *col,
+                               int32_t *cnt, int64_t cap) {
+    if (!rows) return -2;
+    return make_transfer_rows(s, tri_face, npatches_all, center, face, child1, child2, split_axis,
+                              split_dist, leaf_index, face_root, fnormal, fu, dirs_local, k,
+                              threads, rows, nrows, row_ptr, col, cnt, cap);
+}
+
 /* ------------------------------------------------------------------ */
 /* bounce (absent in the reference; project semantics), float64        */
 /* ------------------------------------------------------------------ */
@@ -1570,29 +1718,54 @@ int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t 
  *   per bounce: add_i = sum_j w_ij emit_j ; total_i += add_i ; emit_i = refl_i * add_i
  *   delta = sum_i |add_i|_1 / sum_i |total_i|_1 ; stop after the bounce
  *   whose delta < tol, or after max_bounces.  Returns bounces run. */
+typedef struct {
+    const int64_t *row_ptr;
+    const int32_t *col;
+    const float *w;
+    const double *emit;
+    double *add;
+} spmv_job;
+
+/* add_i = sum_j w_ij emit_j for rows [b, e), each row summed in entry order */
+static void spmv_range(void *ctx, int64_t b, int64_t e, int wk) {
+    (void)wk;
+    const spmv_job *j = (const spmv_job *)ctx;
+    for (int64_t i = b; i < e; i++) {
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int64_t k = j->row_ptr[i]; k < j->row_ptr[i + 1]; k++) {
+            const double wv = (double)j->w[k];
+            const double *em = j->emit + 3 * (int64_t)j->col[k];
+            acc[0] += wv * em[0];
+            acc[1] += wv * em[1];
+            acc[2] += wv * em[2];
+        }
+        for (int c = 0; c < 3; c++) j->add[3 * i + c] = acc[c];
+    }
+}
+
 int orc_bounce_f64(int64_t nrows, const int64_t *row_ptr, const int32_t *col, const float *w,
                    const float *refl, const float *direct, const float *base, int max_bounces,
                    double tol, double *out_total, double *out_deltas) {
+    return orc_bounce_f64_mt(nrows, row_ptr, col, w, refl, direct, base, max_bounces, tol,
+                             out_total, out_deltas, 1);
+}
+
+/* The same, rows spread over `threads` (each row's sum and the energy sums
+ * keep their order, so the result does not depend on the thread count). */
+int orc_bounce_f64_mt(int64_t nrows, const int64_t *row_ptr, const int32_t *col, const float *w,
+                      const float *refl, const float *direct, const float *base, int max_bounces,
+                      double tol, double *out_total, double *out_deltas, int threads) {
     double *emit = malloc(sizeof(double) * 3 * (size_t)(nrows ? nrows : 1));
     double *add = malloc(sizeof(double) * 3 * (size_t)(nrows ? nrows : 1));
     for (int64_t i = 0; i < 3 * nrows; i++) {
         emit[i] = (double)refl[i] * (double)direct[i] + (double)base[i];
         out_total[i] = 0.0;
     }
+    spmv_job j = {row_ptr, col, w, emit, add};
     int b;
     for (b = 0; b < max_bounces; b++) {
         double sa = 0.0, st = 0.0;
-        for (int64_t i = 0; i < nrows; i++) {
-            double acc[3] = {0.0, 0.0, 0.0};
-            for (int64_t e = row_ptr[i]; e < row_ptr[i + 1]; e++) {
-                double wv = (double)w[e];
-                const double *em = emit + 3 * (int64_t)col[e];
-                acc[0] += wv * em[0];
-                acc[1] += wv * em[1];
-                acc[2] += wv * em[2];
-            }
-            for (int c = 0; c < 3; c++) add[3 * i + c] = acc[c];
-        }
+        parallel_for(nrows, threads, 256, spmv_range, &j);
         for (int64_t i = 0; i < 3 * nrows; i++) {
             out_total[i] += add[i];
             emit[i] = (double)refl[i] * add[i];

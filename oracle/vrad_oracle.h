@@ -42,6 +42,10 @@ extern "C" {
 #define ORC_TRACE_ID_SKY        0x01000000
 #define ORC_TRACE_ID_OPAQUE     0x02000000
 #define ORC_TRACE_ID_STATICPROP 0x04000000
+/* Triangle flag of a transparent triangle (the NFlags byte of
+ * raytracer/cache/triangle/trigeometrydata.go:8; the reference defines no
+ * bit, the project uses bit 0). */
+#define ORC_TRI_TRANSPARENT 0x01
 
 #define ORC_MODE_FIXED   0
 #define ORC_MODE_LITERAL 1
@@ -160,6 +164,29 @@ int64_t orc_make_patches(const float *corner, const float *u, const float *v, co
                          int32_t *parent, int32_t *child1, int32_t *child2, int32_t *split_axis,
                          float *split_dist, int32_t *leaf_index);
 
+/* ---- transparent shadows (project semantics) ----
+ * The reference's Trace4Rays takes a transparent-triangle callback
+ * (raytracer/environment.go:140-142) whose one counting implementation adds
+ * each hit triangle's colour x as coverage and clamps at 1
+ * (raytracer/types/coverageCount.go:27-41); texture coverage is a stub
+ * (rad/staticprops/compute.go:4-12).  The reference never fixes the order in
+ * which hits reach the callback.  Here: a triangle with ORC_TRI_TRANSPARENT
+ * in its flags is transparent with coverage cover[i] (the caller passes the
+ * colours' x); a ray's accepted hits are taken in ascending (t, triangle
+ * index): an opaque hit is recorded and ends the walk, a transparent one
+ * adds c = min(c + cover, 1) and, when c reaches 1, is recorded and ends it.
+ * orc_trace_coverage returns the recorded hit, its t and c;
+ * orc_test_lines_coverage is TestLineDoesHitSky with texture shadows
+ * (raytracer/trace/testline.go:29-33,53-55): occlusion = max(opaque, c),
+ * clamped, fraction visible = 1 - occlusion.  Brute force over all
+ * triangles (small scenes only). */
+void orc_trace_coverage(const orc_scene *s, const float *cover, const float *orig, const float *dir,
+                        const float *tmin, const float *tmax, int64_t n, int32_t skip_id,
+                        int threads, int32_t *out_hit, float *out_t, float *out_coverage);
+void orc_test_lines_coverage(const orc_scene *s, const float *cover, const float *start,
+                             const float *stop, int64_t n, int32_t skip_id, int threads,
+                             float *out_frac);
+
 /* ---- transfers ---- */
 /* Per leaf patch, K rays along dirs_local (lx,ly,lz) in the frame (T1,T2,N);
  * counts closest hits per target leaf patch.  Rows are written into the
@@ -173,11 +200,25 @@ int64_t orc_make_transfers(const orc_scene *s, const int32_t *tri_face, int64_t 
                            const float *fnormal, const float *fu,
                            const float *dirs_local, int32_t k, int threads,
                            int64_t *row_ptr, int32_t *col, int32_t *cnt, int64_t cap);
+/* The same rows for a subset of leaf rows (dense indices `rows[0..nrows)`, in
+ * that order): row_ptr[nrows+1] and col/cnt as above.  -1: cap too small;
+ * -2: a row index out of range. */
+int64_t orc_make_transfer_rows(const orc_scene *s, const int32_t *tri_face, int64_t npatches_all,
+                               const float *center, const int32_t *face, const int32_t *child1,
+                               const int32_t *child2, const int32_t *split_axis,
+                               const float *split_dist, const int32_t *leaf_index,
+                               const int32_t *face_root, const float *fnormal, const float *fu,
+                               const float *dirs_local, int32_t k, int threads,
+                               const int64_t *rows, int64_t nrows, int64_t *row_ptr, int32_t *col,
+                               int32_t *cnt, int64_t cap);
 
 /* ---- bounce (float64) ---- */
 int orc_bounce_f64(int64_t nrows, const int64_t *row_ptr, const int32_t *col, const float *w,
                    const float *refl, const float *direct, const float *base, int max_bounces,
                    double tol, double *out_total, double *out_deltas);
+int orc_bounce_f64_mt(int64_t nrows, const int64_t *row_ptr, const int32_t *col, const float *w,
+                      const float *refl, const float *direct, const float *base, int max_bounces,
+                      double tol, double *out_total, double *out_deltas, int threads);
 
 /* ---- lightmap samples ---- */
 /* Shared-exponent sample (r | g << 8 | b << 16 | exponent << 24) of one light. */

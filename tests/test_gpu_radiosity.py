@@ -79,3 +79,25 @@ def test_bounce_repeatable(radiosity):
     t1, b1, _ = r["env"].bounce_light(nl, 20, 1e-3)
     t2, b2, _ = r["env"].bounce_light(nl, 20, 1e-3)
     assert b1 == b2 and np.array_equal(t1, t2)
+
+
+def test_transfers_overflow_path_identical(gpu_ctx, radiosity):
+    # a low table limit sends most rows to the global-memory sort; the CSR
+    # must not change
+    from vrad_gb300 import scenes
+
+    r = radiosity
+    env = r["env"]
+    try:
+        gpu_ctx.set_transfer_table_limit(16)
+        nnz = env.make_transfers(scenes.transfer_directions(r["k"]))
+        k, nnz2, ovf = env.transfer_info()
+        assert (k, nnz2) == (r["k"], nnz) and ovf > 0
+        row_ptr, col, w = env.get_transfers(r["P"]["n_leaves"], nnz)
+    finally:
+        gpu_ctx.set_transfer_table_limit(7168)
+        env.make_transfers(scenes.transfer_directions(r["k"]))
+    assert np.array_equal(row_ptr, r["orow"])
+    assert np.array_equal(col, r["ocol"])
+    assert np.array_equal(w, (r["ocnt"] / np.float32(r["k"])).astype(np.float32))
+    assert env.transfer_info()[2] == 0

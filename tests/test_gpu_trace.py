@@ -83,6 +83,31 @@ def test_trace4rays_soa(env0, oscene0, anyhit_scene):
     hit, dist, nrm = env0.Trace4Rays(a.T.copy(), d.T.copy(), np.zeros(4, np.float32), ln)
     rh, rt = oscene0.trace_closest(a, d, 0.0, ln)
     assert hit.tolist() == rh.tolist() and bits_equal(dist, rt)
+    # SurfaceNormal (raytracer/types/result.go:9): the hit triangle's plane
+    # normal from its intersection record, zero for a miss
+    recs = oscene0.tri_records().view(np.float32)
+    assert (hit >= 0).any()
+    for i in range(4):
+        want = recs[hit[i], :3] if hit[i] >= 0 else np.zeros(3, np.float32)
+        assert bits_equal(np.asarray(nrm).reshape(3, 4)[:, i].copy(), want.copy())
+
+
+def test_trace4rays_surface_normal_many(env0, oscene0):
+    # 4-ray packets from random points, some with tmax short enough to miss
+    rng = np.random.default_rng(7)
+    recs = oscene0.tri_records().view(np.float32)
+    for _ in range(64):
+        o = rng.uniform(1, 4095, (4, 3)).astype(np.float32)
+        d = rng.normal(size=(4, 3)).astype(np.float32)
+        d /= np.sqrt((d * d).sum(1, keepdims=True)).astype(np.float32)
+        tmax = np.array([60000.0, 60000.0, 5.0, 0.5], np.float32)
+        hit, dist, nrm = env0.Trace4Rays(o.T.copy(), d.T.copy(), np.zeros(4, np.float32), tmax)
+        rh, rt = oscene0.trace_closest(o, d, 0.0, tmax)
+        assert hit.tolist() == rh.tolist()
+        nrm = np.asarray(nrm).reshape(3, 4)
+        for i in range(4):
+            want = recs[hit[i], :3] if hit[i] >= 0 else np.zeros(3, np.float32)
+            assert bits_equal(nrm[:, i].copy(), want.copy())
 
 
 def test_test_line_does_hit_sky_with_sky_ceiling(gpu_ctx, oracle, lit_scene):

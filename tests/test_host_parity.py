@@ -296,3 +296,23 @@ def test_wall_slots_and_their_shortcut_keep_the_verdicts(oracle, host_ctx):
     f_walls = s.test_lines(a, b, threads=16)
     s.set_walls()
     assert np.array_equal(f_walls, s.test_lines(a, b, threads=16))
+
+
+def test_set_triangle_flags_errors(host_ctx):
+    from vrad_gb300 import scenes
+    from vrad_gb300._lib import VrgError
+    from vrad_gb300.environment import Environment
+
+    sc = scenes.anyhit_scene(1, n_boxes=4, n_rays=16)
+    xyz, ids = sc.xyz, sc.ids
+    flags = np.zeros(len(ids), np.uint8)
+    flags[12:] = 1
+    colours = np.full((len(ids), 3), 0.5, np.float32)
+    env = Environment(host_ctx)
+    env.add_triangles(xyz, ids)
+    with pytest.raises(VrgError):
+        env.set_triangle_flags(len(ids) - 2, flags[:4])  # past the last triangle
+    env.set_triangle_flags(0, flags, colours)
+    env.SetupAccelerationStructure()
+    with pytest.raises(VrgError, match="out of order"):
+        env.set_triangle_flags(0, flags)  # after the build

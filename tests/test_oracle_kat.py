@@ -210,6 +210,9 @@ def test_closed_box_converges_to_e_over_one_minus_rho(oracle):
     direct = np.zeros((nl, 3), np.float32)
     total, it, deltas = oracle.bounce_f64(row_ptr, col, w, refl, direct, base, 200, 1e-9)
     np.testing.assert_allclose(total, 1.0 / (1.0 - rho), rtol=1e-6)
+    # the threaded bounce gives the same bits and the same bounce count
+    t4, it4, d4 = oracle.bounce_f64(row_ptr, col, w, refl, direct, base, 200, 1e-9, threads=4)
+    assert it4 == it and np.array_equal(t4, total) and np.array_equal(d4, deltas)
 
 
 def test_parallel_plates_form_factor(oracle):
@@ -265,3 +268,74 @@ def test_tiny_scenes(oracle, n):
     hit, t = s.trace_closest(o, d, 0.0, 100.0)
     h2, t2 = s.trace_closest(o, d, 0.0, 100.0, brute=True)
     assert hit.tolist() == h2.tolist() and bits_equal(t, t2)
+
+
+def test_transfer_rows_subset_equals_full_build(oracle):
+    # the row-subset builder that checks sampled rows at full size gives the
+    # rows of the full build
+    from conftest import small_lit_scene
+    from vrad_gb300 import scenes
+
+    lit = small_lit_scene(40, seed=11)
+    s = oracle.Scene(lit.xyz, lit.ids)
+    P = oracle.make_patches(lit)
+    dirs = scenes.transfer_directions(256)
+    row_ptr, col, cnt = oracle.make_transfers(s, lit, P, dirs, threads=4)
+    nl = len(row_ptr) - 1
+    rows = np.array([nl - 1, 0, 3, nl // 2], np.int64)
+    sp, sc, sn = oracle.make_transfer_rows(s, lit, P, dirs, rows, threads=4)
+    for j, r in enumerate(rows):
+        assert np.array_equal(sc[sp[j]:sp[j + 1]], col[row_ptr[r]:row_ptr[r + 1]])
+        assert np.array_equal(sn[sp[j]:sp[j + 1]], cnt[row_ptr[r]:row_ptr[r + 1]])
+    with pytest.raises(ValueError):
+        oracle.make_transfer_rows(s, lit, P, dirs, np.array([nl], np.int64))
+
+
+def _layer_scene(layers):
+    """Squares [0,100]^2 at the given z, each two triangles (AddQuad split);
+    layers: (z, id, flags, coverage)."""
+    xyz, ids, flags, cover = [], [], [], []
+    for z, tid, fl, cv in layers:
+        v1, v2, v3, v4 = (0, 0, z), (100, 0, z), (100, 100, z), (0, 100, z)
+        for tri in ((v1, v2, v3), (v1, v3, v4)):
+            xyz.append([c for v in tri for c in v])
+            ids.append(tid)
+            flags.append(fl)
+            cover.append(cv)
+    return (np.array(xyz, np.float32), np.array(ids, np.int32), np.array(flags, np.uint8),
+            np.array(cover, np.float32))
+
+
+def test_transparent_coverage_known_answers(oracle):
+    T, OPAQUE, SKY = 1, 0x02000000, 0x01000000
+    xyz, ids, fl, cv = _layer_scene([(10, OPAQUE, T, 0.25), (20, OPAQUE, T, 0.5),
+                                     (30, OPAQUE, T, 0.5), (40, OPAQUE, 0, 0.9)])
+    s = oracle.Scene(xyz, ids, flags=fl)
+    a = np.array([[30, 60, 0]] * 3, np.float32)
+    b = np.array([[30, 60, 25], [30, 60, 50], [30, 60, 35]], np.float32)
+    frac = s.test_lines_coverage(cv, a, b, threads=1)
+    # 0.25 + 0.5 = 0.75 before z=25; the third layer takes it to 1
+    assert frac.tolist() == [0.25, 0.0, 0.0]
+    d = np.array([[0, 0, 1]] * 3, np.float32)
+    hit, t, cov = s.trace_coverage(cv, a, d, 0.0, np.array([25, 50, 35], np.float32), threads=1)
+    # coverage reaches 1 at the third layer (z = 30, triangle 5 of the (v1,v3,v4) halves)
+    assert hit.tolist() == [-1, 5, 5] and t.tolist()[1:] == [30.0, 30.0]
+    assert cov.tolist() == [0.75, 1.0, 1.0]
+    # lighter layers: the opaque layer is reached and recorded; a sky layer
+    # there lets the coverage through
+    for top_id, want in ((OPAQUE, 0.0), (SKY, 0.375)):
+        xyz, ids, fl, cv = _layer_scene([(10, OPAQUE, T, 0.125), (20, OPAQUE, T, 0.25),
+                                         (30, OPAQUE, T, 0.25), (40, top_id, 0, 0.9)])
+        s = oracle.Scene(xyz, ids, flags=fl)
+        assert s.test_lines_coverage(cv, a[:1], [[30, 60, 50]]).tolist() == [want]
+        hit, t, cov = s.trace_coverage(cv, a[:1], d[:1], 0.0, 50.0)
+        assert hit.tolist() == [7] and t.tolist() == [40.0] and cov.tolist() == [0.625]
+    # without the transparent flag a layer is an ordinary occluder; a layer
+    # whose id is skipped is not seen at all; a zero-length line is visible
+    xyz, ids, fl, cv = _layer_scene([(10, OPAQUE, 0, 0.25), (20, 0x04000007, T, 0.5)])
+    s = oracle.Scene(xyz, ids, flags=fl)
+    assert s.test_lines_coverage(cv, a[:1], [[30, 60, 50]]).tolist() == [0.0]
+    s2 = oracle.Scene(xyz[2:], ids[2:], flags=fl[2:])
+    assert s2.test_lines_coverage(cv[2:], a[:1], [[30, 60, 50]], skip=0x04000007).tolist() == [1.0]
+    assert s2.test_lines_coverage(cv[2:], a[:1], [[30, 60, 50]]).tolist() == [0.5]
+    assert s2.test_lines_coverage(cv[2:], a[:1], a[:1]).tolist() == [1.0]

@@ -60,6 +60,9 @@ SIGNATURES = {
     "vrg_env_trace_closest_d": (C.c_int, [P, P, P, P, P, I64, I32, P, P]),
     "vrg_env_test_line_does_hit_sky": (C.c_int, [P, P, P, I64, I32, P]),
     "vrg_env_occlusion_mask": (C.c_int, [P, P, P, I64, I32, P, P, P]),
+    "vrg_env_trace_coverage": (C.c_int, [P, P, P, P, P, I64, I32, P, P, P]),
+    "vrg_env_test_line_coverage": (C.c_int, [P, P, P, I64, I32, P]),
+    "vrg_env_set_triangle_flags": (C.c_int, [P, I64, I64, P, P]),
     "vrg_env_occlusion_mask_d": (C.c_int, [P, P, P, I64, I32, P, P, P]),
     "vrg_env_add_to_ray_stream": (C.c_int, [P, P, P, I32]),
     "vrg_env_flush_stream_entry": (C.c_int, [P]),
@@ -77,6 +80,8 @@ SIGNATURES = {
     "vrg_env_get_patches": (C.c_int, [P, P, P, P, P, P, P, P, P, P, P, P]),
     "vrg_env_make_transfers": (C.c_int, [P, P, I32, P]),
     "vrg_env_get_transfers": (C.c_int, [P, P, P, P]),
+    "vrg_env_transfer_info": (C.c_int, [P, P, P, P]),
+    "vrg_ctx_set_transfer_table_limit": (C.c_int, [P, I32]),
     "vrg_env_gather_patch_direct": (C.c_int, [P, P]),
     "vrg_env_bounce_light": (C.c_int, [P, I32, F, P, P, P]),
     "vrg_env_bounce_light_noalloc": (C.c_int, [P, I32, F, P, P, P]),

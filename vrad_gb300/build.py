@@ -20,7 +20,7 @@ LIB = OUT / "libvradgpu.so"
 PROBE = OUT / "libvrgprobe.so"  # bench-only L2 bandwidth probe
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_EXACT = ["trace.cu", "direct.cu", "transfer.cu", "batch.cu", "relight.cu", "lightmap.cu"]
+CU_EXACT = ["trace.cu", "direct.cu", "transfer.cu", "batch.cu", "relight.cu", "lightmap.cu", "coverage.cu"]
 CU_FAST = ["bounce.cu", "kdbuild_gpu.cu"]
 CPP = ["capi.cpp", "environment.cpp", "kdbuild.cpp", "lights.cpp", "patches.cpp", "tune.cpp", "bsp.cpp", "bsp_file.cpp"]
 

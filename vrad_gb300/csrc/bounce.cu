@@ -298,8 +298,11 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
 // from vrg_env_make_transfers and the patch direct light from
 // vrg_env_gather_patch_direct) and keeps its working state (two emission
 // buffers, per-block partial sums, the loop control block) in one
-// file-scope device array, allocated once when the library's device code is
-// loaded and held until the process exits.
+// file-scope device array, held by every GPU that loads the library until
+// the process exits.  With lazy module loading the array comes into being
+// when bounce.cu's module is first loaded on a device; vrg_ctx_create does
+// that (noalloc_prepare below), so the entry point itself allocates
+// nothing, its first call included.
 namespace vrg {
 namespace {
 
@@ -342,6 +345,20 @@ void count_launch(vrg_ctx *ctx) {
 }
 
 }  // namespace
+
+// Context set-up (device current): resolves the scratch array's address and
+// loads the no-alloc path's kernels, so neither happens inside a later call.
+int noalloc_prepare(vrg_ctx *ctx) {
+    NoAllocScratch *sc = nullptr;
+    const int rc = noalloc_scratch(ctx, &sc);
+    if (rc != VRG_OK) return rc;
+    cudaFuncAttributes fa;
+    VRG_CUDA(ctx, cudaFuncGetAttributes(&fa, k_bounce_init));
+    VRG_CUDA(ctx, cudaFuncGetAttributes(&fa, k_bounce_spmv<4>));
+    VRG_CUDA(ctx, cudaFuncGetAttributes(&fa, k_bounce_reduce));
+    return VRG_OK;
+}
+
 }  // namespace vrg
 
 extern "C" int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, float rel_tol,
@@ -350,19 +367,35 @@ extern "C" int vrg_env_bounce_light_noalloc(vrg_env *env, int32_t max_bounces, f
     using namespace vrg;
     if (!env) return VRG_ERR_INVALID;
     vrg_ctx *ctx = env->ctx;
+    std::lock_guard<std::mutex> lk(env->mu);
     if (ctx->host_only) return fail(ctx, VRG_ERR_STATE, "host-only context has no device");
     if (!env->built || !env->have_transfers)
         return fail(ctx, VRG_ERR_STATE, "vrg_env_make_transfers has not run");
     if (!env->have_patch_direct)
         return fail(ctx, VRG_ERR_STATE, "vrg_env_gather_patch_direct has not run");
-    if (max_bounces < 0 || !(rel_tol >= 0.0f) || !total_out) return VRG_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(env->mu);
+    if (max_bounces < 0 || !(rel_tol >= 0.0f) || !total_out)
+        return fail(ctx, VRG_ERR_INVALID, "no-alloc bounce: bad bounce count, tolerance or output");
     const int64_t n = (int64_t)env->patches.leaf_patch.size();
     if (n > kNoAllocMaxRows)
         return fail(ctx, VRG_ERR_UNSUPPORTED,
                     "no-alloc bounce holds at most 262144 leaf patches; this scene has " +
                         std::to_string(n));
     VRG_CUDA(ctx, cudaSetDevice(ctx->device));
+    // The output is written as float4: it must be device (or managed) memory
+    // of this context's device, 16-byte aligned.  Anything else would fault
+    // on the GPU, so it is refused here, before any launch.
+    {
+        cudaPointerAttributes pa{};
+        const cudaError_t e = cudaPointerGetAttributes(&pa, total_out);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, VRG_ERR_INVALID, "no-alloc bounce: total_out is not a device pointer");
+        }
+        if ((pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) || pa.device != ctx->device)
+            return fail(ctx, VRG_ERR_INVALID, "no-alloc bounce: total_out is not device memory of this context's GPU");
+        if ((reinterpret_cast<uintptr_t>(total_out) & 15u) != 0)
+            return fail(ctx, VRG_ERR_INVALID, "no-alloc bounce: total_out is not 16-byte aligned");
+    }
     NoAllocScratch *sc = nullptr;
     {
         const int rc = noalloc_scratch(ctx, &sc);

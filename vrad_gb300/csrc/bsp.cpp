@@ -343,6 +343,8 @@ int vrg_env_add_bsp_world(vrg_env *env, const vrg_bsp_world *world, int64_t *bru
         std::lock_guard<std::mutex> lk(env->mu);
         if (env->built) return fail(env->ctx, VRG_ERR_STATE, "triangles added after SetupAccelerationStructure");
         const size_t n = ids.size();
+        env->cover.resize(env->ids.size(), 0.0f);
+        env->cover.insert(env->cover.end(), n, 1.0f);  // fullCoverage's x
         env->xyz.insert(env->xyz.end(), xyz.begin(), xyz.end());
         env->ids.insert(env->ids.end(), ids.begin(), ids.end());
         env->flags.insert(env->flags.end(), n, 0);

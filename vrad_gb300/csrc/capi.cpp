@@ -157,6 +157,9 @@ int vrg_ctx_create(int device, vrg_ctx **out) {
         return e == cudaErrorMemoryAllocation ? VRG_ERR_NOMEM : VRG_ERR_CUDA;
     }
     ctx->stream = ctx->own_stream;
+    // the no-alloc bounce's device array and kernels are set up now, so that
+    // its calls allocate nothing; a failure here is reported by that call
+    if (vrg::noalloc_prepare(ctx) != VRG_OK) ctx->last_error.clear();
     *out = ctx;
     return VRG_OK;
 }
@@ -260,7 +263,12 @@ int vrg_env_add_triangle(vrg_env *env, int32_t id, const float *v1, const float 
     env->xyz.insert(env->xyz.end(), v2, v2 + 3);
     env->xyz.insert(env->xyz.end(), v3, v3 + 3);
     env->ids.push_back(id);
+    env->flags.resize(env->ids.size() - 1, 0);
     env->flags.push_back((uint8_t)flags);
+    // coverage of the triangle when it is transparent: its colour's x, as
+    // types.CoverageCount adds it (raytracer/types/coverageCount.go:27-41)
+    env->cover.resize(env->ids.size() - 1, 0.0f);
+    env->cover.push_back(colour ? colour[0] : 0.0f);
     // environment.go:61-66: colours and materials unless the flags say not to
     if (!(flags & VRG_RTE_FLAGS_DONT_STORE_TRIANGLE_COLORS)) {
         const float zero[3] = {0, 0, 0};
@@ -820,12 +828,28 @@ int vrg_env_get_patches(const vrg_env *env, float *mins, float *maxs, float *cen
 int vrg_env_make_transfers(vrg_env *env, const float *dirs_local, int32_t k, int64_t *out_nnz) {
     TRY(need_built(env));
     if (!env->have_patches) return fail(env->ctx, VRG_ERR_STATE, "MakePatches has not run");
-    if (!dirs_local || k < 32 || k > 16384 || (k & (k - 1)) != 0)
-        return fail(env->ctx, VRG_ERR_UNSUPPORTED, "transfer ray count must be a power of two in [32, 16384]");
+    if (!dirs_local || k < 32 || k > 65536 || (k & (k - 1)) != 0)
+        return fail(env->ctx, VRG_ERR_UNSUPPORTED, "transfer ray count must be a power of two in [32, 65536]");
     std::lock_guard<std::mutex> lk(env->mu);
     env->relight_ready = false;
     TRY(run_make_transfers(env, dirs_local, k));
     if (out_nnz) *out_nnz = env->nnz;
+    return VRG_OK;
+}
+
+int vrg_env_transfer_info(const vrg_env *env, int32_t *k, int64_t *nnz, int64_t *overflow_rows) {
+    if (!env || !env->have_transfers) return VRG_ERR_STATE;
+    std::lock_guard<std::mutex> lk(env->mu);
+    if (k) *k = env->transfer_k;
+    if (nnz) *nnz = env->nnz;
+    if (overflow_rows) *overflow_rows = env->transfer_overflow_rows;
+    return VRG_OK;
+}
+
+int vrg_ctx_set_transfer_table_limit(vrg_ctx *ctx, int32_t limit) {
+    if (!ctx || limit < 1) return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->xfer_table_limit = std::min<int32_t>(limit, 7168);
     return VRG_OK;
 }
 

@@ -241,6 +241,7 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         for (std::thread &t : pool) t.join();
     }
     env->built = true;
+    env->cover_ready = false;
     if (ctx->host_only) return VRG_OK;
     VRG_CUDA(ctx, cudaSetDevice(ctx->device));
     VRG_CUDA(ctx, env->d_nodes.reserve(nn * sizeof(uint2)));
@@ -259,6 +260,7 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
                                       cudaMemcpyHostToDevice, ctx->stream));
     VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     env->built = true;
+    env->cover_ready = false;
     return VRG_OK;
 }
 

@@ -7,7 +7,7 @@ looks for sky.  This script parses the Go literals and writes them out as a C
 array with the decimal text unchanged, so a C compiler rounds each literal to
 float32 exactly as Go's constant conversion does.
 
-Usage:  python vrad_gb300/csrc/gen_anorms.py /root/reference/vmath/constants.go
+Usage:  python vrad_gb300/csrc/gen_anorms.py <reference checkout>/vmath/constants.go
 The generated header is committed; the GPU build never needs the reference.
 """
 import re
@@ -42,7 +42,9 @@ def render(vecs) -> str:
 
 
 def main():
-    src = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/vmath/constants.go")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: gen_anorms.py <path to the reference's vmath/constants.go>")
+    src = Path(sys.argv[1])
     out = Path(__file__).with_name("anorms_table.h")
     out.write_text(render(parse(src.read_text())))
     print(f"wrote {out}")

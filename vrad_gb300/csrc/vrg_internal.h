@@ -85,6 +85,7 @@ struct vrg_ctx {
     int64_t launches = 0;
     bool autotune = true;
     uint64_t hbm_reserve = (uint64_t)1 << 30;  // kept free when admitting a relight scene
+    int32_t xfer_table_limit = 7168;            // distinct targets per transfer row held in shared memory
     std::map<std::string, int> tuned;                   // bucket key -> variant
     std::map<std::string, std::vector<double>> tune_ms;  // bucket key -> variant times
 };
@@ -127,6 +128,7 @@ struct vrg_env {
     std::vector<int32_t> ids;
     std::vector<uint8_t> flags;
     std::vector<float> colours;
+    std::vector<float> cover;  // per triangle: colour x, the coverage of a transparent triangle
     std::vector<int32_t> materials;
     float min_bound[3] = {0, 0, 0}, max_bound[3] = {0, 0, 0};
 
@@ -146,6 +148,11 @@ struct vrg_env {
     vrg::DevBuf d_top;       // top levels of the tree (kTopNodes entries at most)
     uint32_t ntop = 0;
 
+    // transparent shadows (coverage.cu): per-triangle flags and coverage
+    vrg::DevBuf d_tri_flags, d_tri_cover;
+    bool cover_ready = false;
+    int32_t n_transparent = 0;
+
     // lights
     std::vector<vrg_light> lights;
     vrg::DevBuf d_lights;
@@ -164,6 +171,7 @@ struct vrg_env {
     bool have_transfers = false;
     int64_t nnz = 0;
     int32_t transfer_k = 0;
+    int64_t transfer_overflow_rows = 0;  // rows of the last build past the shared-memory row table
     vrg::DevBuf d_row_ptr, d_col, d_weight;
     vrg::DevBuf d_leaf_direct;
     bool have_patch_direct = false;
@@ -256,5 +264,6 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
                float *delta);
 void relight_release(vrg_env *env);
 void bounce_release(vrg_env *env);
+int noalloc_prepare(vrg_ctx *ctx);  // bounce.cu: the no-alloc bounce's array and kernels
 
 }  // namespace vrg

@@ -85,6 +85,10 @@ class Context:
     def launch_count(self) -> int:
         return int(self.lib.vrg_ctx_launch_count(self.h))
 
+    def set_transfer_table_limit(self, limit: int):
+        check(self.lib.vrg_ctx_set_transfer_table_limit(self.h, int(limit)), self.h,
+              "set_transfer_table_limit")
+
     def set_hbm_reserve(self, nbytes: int):
         """Device memory that relight admission keeps free (default 1 GiB)."""
         check(self.lib.vrg_ctx_set_hbm_reserve(self.h, int(nbytes)), self.h, "set_hbm_reserve")
@@ -417,6 +421,36 @@ class Environment:
                                                  _p(hit), _p(t)), "trace_closest")
         return hit, t
 
+    def set_triangle_flags(self, first, flags, colours=None):
+        """Flags (VRG_TRIFLAG_TRANSPARENT = 1) and colours of triangles
+        [first, first + len(flags)); colour x is a transparent triangle's
+        coverage."""
+        fl = np.ascontiguousarray(flags, np.uint8)
+        col = None if colours is None else _f32(colours, (-1, 3))
+        self._chk(self.lib.vrg_env_set_triangle_flags(self.h, int(first), fl.size, _p(fl),
+                                                      _p(col)), "set_triangle_flags")
+
+    def trace_coverage(self, origin, direction, tmin, tmax, skip_id=-1):
+        """Trace4Rays with a coverage-counting transparency callback: per ray
+        the recorded hit, its t and the coverage."""
+        o, d = _f32(origin, (-1, 3)), _f32(direction, (-1, 3))
+        n = o.shape[0]
+        t0 = _f32(np.broadcast_to(np.float32(tmin) if np.isscalar(tmin) else tmin, (n,)))
+        t1 = _f32(np.broadcast_to(np.float32(tmax) if np.isscalar(tmax) else tmax, (n,)))
+        hit, t, cov = np.empty(n, np.int32), np.empty(n, np.float32), np.empty(n, np.float32)
+        self._chk(self.lib.vrg_env_trace_coverage(self.h, _p(o), _p(d), _p(t0), _p(t1), n, skip_id,
+                                                  _p(hit), _p(t), _p(cov)), "trace_coverage")
+        return hit, t, cov
+
+    def test_line_coverage(self, start, stop, static_prop_to_skip=-1):
+        """TestLineDoesHitSky with texture shadows (transparent coverage)."""
+        a, b = _f32(start, (-1, 3)), _f32(stop, (-1, 3))
+        out = np.empty(a.shape[0], np.float32)
+        self._chk(self.lib.vrg_env_test_line_coverage(self.h, _p(a), _p(b), a.shape[0],
+                                                      static_prop_to_skip, _p(out)),
+                  "test_line_coverage")
+        return out
+
     def test_line_does_hit_sky(self, start, stop, static_prop_to_skip=-1):
         a, b = _f32(start, (-1, 3)), _f32(stop, (-1, 3))
         out = np.empty(a.shape[0], np.float32)
@@ -520,6 +554,13 @@ class Environment:
         self._chk(self.lib.vrg_env_make_transfers(self.h, _p(d), d.shape[0], C.byref(nnz)),
                   "make_transfers")
         return nnz.value
+
+    def transfer_info(self):
+        """(k, nnz, rows past the shared-memory row table) of the last build."""
+        k, nnz, ovf = C.c_int32(), C.c_int64(), C.c_int64()
+        self._chk(self.lib.vrg_env_transfer_info(self.h, C.byref(k), C.byref(nnz), C.byref(ovf)),
+                  "transfer_info")
+        return k.value, nnz.value, ovf.value
 
     def get_transfers(self, n_leaves, nnz):
         row_ptr = np.zeros(n_leaves + 1, np.int64)
