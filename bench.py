@@ -9,6 +9,8 @@ compared luxel by luxel against the oracle (`parity`).
 The same JSON line carries the rest of the metric, one object per workload,
 each with its own error against the oracle and its roofline:
   anyhit     2^20 shadow lines, 12,300 triangles: mask and closest-hit Mrays/s
+  rooms      the headline bake with the wall slots off, and with the room's
+             walls split into 16 x 16 tiles per face: what the slots buy
   radiosity  the same faces at 64-unit patches, 65,536 transfer rays per
              patch: CSR build, bounce SpMV GB/s, solve to 1e-3
   batch      256 scenes baked together vs one scene per launch: bakes/s
@@ -483,7 +485,7 @@ def run_gpu(args, rank, world, local_rank):
     }
     env.close()
     if not args.headline_only and world == 1:
-        for name, fn in (("anyhit", sub_anyhit), ("radiosity", sub_radiosity),
+        for name, fn in (("anyhit", sub_anyhit), ("rooms", sub_rooms), ("radiosity", sub_radiosity),
                          ("batch", sub_batch), ("serve", sub_serve)):
             t0 = time.perf_counter()
             try:
@@ -606,6 +608,70 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
                          "kind": "port", "sample": f"all {n} lines, the reference's SAH tree"},
         "clocks": clk,
     }
+
+
+def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
+    """What the wall slots buy.  The headline's box room has six walls of two
+    triangles each, so most sky lines end on a wall slot test.  Here the same
+    bake runs with the slots off, and on the same scene with each room face
+    split into 16 x 16 tiles (as a map's brush sides make walls: the slots
+    then hold 4 of 512 triangles per face), with and without the slots; the
+    tiled room's luxels of faces 0-255 are checked against the oracle."""
+    import torch
+
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    from vrad_gb300.environment import Context
+
+    out = {}
+    got_tiled = None
+    for name, tiles, slots in (("box_room_slots_off", 1, False), ("tiled_16x16_slots_on", 16, True),
+                               ("tiled_16x16_slots_off", 16, False)):
+        # a context of its own per room, so that each is autotuned on itself
+        ctx = Context(dev.index)
+        ctx.set_stream(stream.cuda_stream)
+        lib = ctx.lib
+        lit = scenes.lit_scene(SEED, wall_tiles=tiles)
+        env = Environment(ctx)
+        env.set_wall_slots(slots)
+        env.add_triangles(lit.xyz, lit.ids)
+        env.SetupAccelerationStructure()
+        env.set_faces(lit)
+        env.set_lights(lit.lights)
+        nlux = env.num_luxels()
+        d_out = torch.empty((nlux, 3), dtype=torch.float32, device=dev)
+        rays = C.c_uint64()
+
+        def bake(want_rays=False):
+            rc = lib.vrg_env_gather_direct_light_d(env.h, 4, SEED, d_out.data_ptr(),
+                                                   C.byref(rays) if want_rays else None)
+            assert rc == 0, rc
+
+        bake(True)
+        for _ in range(2):
+            bake()
+        ms = _event_ms(stream, bake, max(3, args.steps // 2), flush)
+        mean = statistics.mean(ms)
+        tv, tms = ctx.autotune_choice(Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
+        out[name] = {"value": round(rays.value / (mean * 1e-3) / 1e6, 1), "unit": "Mrays/s",
+                     "ms_per_step": round(mean, 3), "rays_per_step": rays.value,
+                     "triangles": len(lit.ids), "wall_slot_triangles_per_face": env.wall_slots()[1].tolist(),
+                     "autotune": {"variant": tv, "variant_ms": [round(x, 3) for x in tms]}}
+        if name == "tiled_16x16_slots_on":
+            got_tiled = (d_out.cpu().numpy(), lit)
+        env.close()
+        ctx.close()
+    from oracle import pyoracle
+
+    got, lit = got_tiled
+    off = lit.luxel_offset()
+    nf = min(256, lit.n_faces)
+    ref, _ = pyoracle.gather_luxels(pyoracle.Scene(lit.xyz, lit.ids), pyoracle.make_lights(lit.lights),
+                                    len(lit.lights), lit, 0, nf, ss=4, seed=SEED,
+                                    threads=os.cpu_count() or 1)
+    out["tiled_parity_faces_0_255"] = rel_error_stats(got[: off[nf]], ref)
+    return out
 
 
 def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
@@ -936,7 +1002,7 @@ def run_one(args, local_rank):
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     l2 = _l2_read_gbs(local_rank)
-    fn = {"anyhit": sub_anyhit, "radiosity": sub_radiosity, "batch": sub_batch,
+    fn = {"anyhit": sub_anyhit, "rooms": sub_rooms, "radiosity": sub_radiosity, "batch": sub_batch,
           "serve": sub_serve}[args.workload]
     rec = fn(args, ctx, stream, dev, flush, l2, sms)
     rec.setdefault("higher_is_better", True)
@@ -952,7 +1018,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="direct",
-                    choices=["direct", "anyhit", "radiosity", "batch", "serve"])
+                    choices=["direct", "anyhit", "rooms", "radiosity", "batch", "serve"])
     ap.add_argument("--headline-only", action="store_true",
                     help="the direct-light line alone, without the other workloads")
     ap.add_argument("--rates", default="50,200,1000,2000", help="request rates of the serve workload")

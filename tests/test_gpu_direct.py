@@ -97,3 +97,29 @@ def test_gather_points_with_fades_and_exponent(gpu_ctx, oracle, lit_scene):
                                       threads=16)
     assert rays == rrays
     assert _rel_err(got, ref).max() <= RTOL
+
+
+def test_tiled_room_with_and_without_wall_slots(gpu_ctx, oracle):
+    # walls split into tiles (as brush sides make them): the gather with the
+    # wall slots, without them, and the oracle give the same luxels
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    lit = scenes.lit_scene(6, n_faces=96, n_point=12, n_spot=4, wall_tiles=8)
+    outs = []
+    for slots in (True, False):
+        env = Environment(gpu_ctx)
+        env.set_wall_slots(slots)
+        env.add_triangles(lit.xyz, lit.ids)
+        env.SetupAccelerationStructure()
+        assert (env.wall_slots()[1] > 0).any() == slots
+        env.set_faces(lit)
+        env.set_lights(lit.lights)
+        outs.append(env.gather_direct_light(supersamples=4, seed=1))
+    assert outs[0][1] == outs[1][1] and np.array_equal(outs[0][0].view(np.uint32),
+                                                       outs[1][0].view(np.uint32))
+    ref, rays = oracle.gather_luxels(oracle.Scene(lit.xyz, lit.ids),
+                                     oracle.make_lights(lit.lights), len(lit.lights), lit, 0,
+                                     lit.n_faces, ss=4, seed=1, threads=16)
+    assert rays == outs[0][1]
+    assert _rel_err(outs[0][0], ref).max() <= RTOL

@@ -54,16 +54,18 @@ __global__ void k_bounce_init(const LeafInfo *__restrict__ info, const float *__
 }
 
 // One warp per row (row_gather with U entries per lane per round), rows
-// strided over the grid's warps.  Per-block sums of |add| and |total| go to
-// partials[2*block].
-template <int U>
-__global__ void __launch_bounds__(kSpmvThreads) k_bounce_spmv(
+// strided over the grid's warps, so the NT / 32 warps of a block work on
+// neighbouring rows (neighbouring patches, which see much the same patches:
+// their emission gathers share L1 lines).  Per-block sums of |add| and
+// |total| go to partials[2*block].
+template <int U, int NT = kSpmvThreads>
+__global__ void __launch_bounds__(NT) k_bounce_spmv(
     const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
     const float *__restrict__ w, const float4 *__restrict__ emit_in, float4 *__restrict__ emit_out,
     float4 *__restrict__ total, const LeafInfo *__restrict__ info, int64_t n,
     const BounceControl *__restrict__ ctl, double *__restrict__ partials) {
     if (*(volatile const int32_t *)&ctl->done) return;
-    __shared__ double red[2][kSpmvThreads / 32];
+    __shared__ double red[2][NT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double sa = 0.0, st = 0.0;
@@ -88,7 +90,7 @@ __global__ void __launch_bounds__(kSpmvThreads) k_bounce_spmv(
     __syncthreads();
     if (threadIdx.x == 0) {
         double a = 0.0, t = 0.0;
-        for (int k = 0; k < kSpmvThreads / 32; k++) {
+        for (int k = 0; k < NT / 32; k++) {
             a += red[0][k];
             t += red[1][k];
         }
@@ -170,25 +172,28 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
     VRG_CUDA(ctx, init());
 
     // SpMV variants, picked per (nnz, rows) bucket: 4, 8 or 2 entries per
-    // lane per round (the same sums).  Each runs one wave: resident blocks
-    // per SM times SMs.
+    // lane per round, and 256, 512 or 1024 threads per block (more
+    // neighbouring rows per block at a time); the same sums.  Each runs one
+    // wave: resident blocks per SM times SMs.
     using SpmvKernel = void (*)(const int64_t *, const int32_t *, const float *, const float4 *,
                                 float4 *, float4 *, const LeafInfo *, int64_t,
                                 const BounceControl *, double *);
-    constexpr int kSpmvVariants = 3;
-    const SpmvKernel kvar[kSpmvVariants] = {k_bounce_spmv<4>, k_bounce_spmv<8>, k_bounce_spmv<2>};
+    constexpr int kSpmvVariants = 6;
+    const SpmvKernel kvar[kSpmvVariants] = {k_bounce_spmv<4>,       k_bounce_spmv<8>,       k_bounce_spmv<2>,
+                                            k_bounce_spmv<4, 512>,  k_bounce_spmv<4, 1024>, k_bounce_spmv<2, 1024>};
+    const int vthreads[kSpmvVariants] = {256, 256, 256, 512, 1024, 1024};
     auto spmv_blocks = [&](int v) {
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kvar[v], kSpmvThreads, 0) != cudaSuccess ||
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kvar[v], vthreads[v], 0) != cudaSuccess ||
             per_sm < 1)
-            per_sm = 2;
+            per_sm = 1;
         return ctx->num_sms * std::min(per_sm, 8);
     };
     auto spmv = [&](int v, float4 *in, float4 *out) -> cudaError_t {
         cudaEvent_t ev2 = nullptr;
         timing_begin(ctx, "bounce_spmv", &ev2);
         const SpmvKernel k = kvar[v];
-        k<<<spmv_blocks(v), kSpmvThreads, 0, ctx->stream>>>(
+        k<<<spmv_blocks(v), vthreads[v], 0, ctx->stream>>>(
             env->d_row_ptr.as<int64_t>(), env->d_col.as<int32_t>(), env->d_weight.as<float>(), in, out,
             env->d_total.as<float4>(), env->d_leaf_info.as<LeafInfo>(), n, ctl, env->d_partials.as<double>());
         cudaError_t e = cudaGetLastError();

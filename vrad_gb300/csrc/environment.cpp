@@ -186,7 +186,7 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     std::vector<int32_t> wall[6];
     {
         std::vector<std::pair<double, int32_t>> cand[6];
-        for (int64_t t = 0; t < n; t++) {
+        for (int64_t t = 0; t < (env->use_wall_slots ? n : 0); t++) {
             if (env->ids[t] & VRG_TRACE_ID_SKY) continue;
             const float *v = &env->xyz[9 * t];
             for (int a = 0; a < 3; a++)
@@ -244,6 +244,14 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     env->cover_ready = false;
     if (ctx->host_only) return VRG_OK;
     VRG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!env->status_h) {
+        void *h = nullptr, *d = nullptr;
+        VRG_CUDA(ctx, cudaHostAlloc(&h, sizeof(uint32_t), cudaHostAllocMapped));
+        env->status_h = static_cast<uint32_t *>(h);
+        VRG_CUDA(ctx, cudaHostGetDevicePointer(&d, h, 0));
+        env->status_d = static_cast<uint32_t *>(d);
+    }
+    *env->status_h = 0;
     VRG_CUDA(ctx, env->d_nodes.reserve(nn * sizeof(uint2)));
     VRG_CUDA(ctx, env->d_leaf_tris.reserve(leaf.size() * sizeof(float4)));
     VRG_CUDA(ctx, env->d_tri_ids.reserve((n ? n : 1) * sizeof(int32_t)));
@@ -322,6 +330,21 @@ int vrg_env_set_walk_tree_builder(vrg_env *env, int32_t mode) {
     std::lock_guard<std::mutex> lk(env->mu);
     if (env->built) return fail(env->ctx, VRG_ERR_STATE, "walk tree builder set after the build");
     env->walk_builder = mode;
+    return VRG_OK;
+}
+
+int vrg_env_set_wall_slots(vrg_env *env, int32_t enable) {
+    if (!env || enable < 0 || enable > 1) return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(env->mu);
+    if (env->built) return fail(env->ctx, VRG_ERR_STATE, "wall slots set after the build");
+    env->use_wall_slots = enable != 0;
+    return VRG_OK;
+}
+
+int vrg_env_set_stack_limit(vrg_env *env, int32_t entries) {
+    if (!env || entries < 1 || entries > vrg::kStackMax) return VRG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(env->mu);
+    env->stack_limit = entries;
     return VRG_OK;
 }
 

@@ -200,20 +200,42 @@ def _unit_vectors(rng: Stream, n: int) -> np.ndarray:
     return np.asarray(out, dtype=np.float32)
 
 
+def _tiled_room(soup: TriangleSoup, tiles: int, sky: bool) -> int:
+    """The room's six faces, each split into tiles x tiles quads in its plane
+    (the way a map's walls arrive as many brush sides), in the box's face
+    order; returns the triangle count."""
+    quads, _ = box_quads((0.0, 0.0, 0.0), (ROOM, ROOM, ROOM))
+    for k, (v1, v2, _v3, v4) in enumerate(quads):
+        a, b, d = (np.asarray(v, np.float64) for v in (v1, v2, v4))
+        tid = TRACE_ID_SKY if (k == 0 and sky) else TRACE_ID_OPAQUE
+        for i in range(tiles):
+            for j in range(tiles):
+                def at(s, t):
+                    return tuple(float(c) for c in (a + (b - a) * (s / tiles) + (d - a) * (t / tiles)))
+                soup.add_quad(tid, at(i, j), at(i + 1, j), at(i + 1, j + 1), at(i, j + 1))
+    return 12 * tiles * tiles
+
+
 def lit_scene(seed: int = 0, n_faces: int = 4096, spacing: float = 16.0, n_point: int = 64,
-              n_spot: int = 8, sky: bool = True, edge=(64.0, 512.0)) -> LitScene:
+              n_spot: int = 8, sky: bool = True, edge=(64.0, 512.0), wall_tiles: int = 1) -> LitScene:
     """Direct-lighting scene: ``ceil(n_faces/6)`` boxes (edges U(64,512))
     whose first ``n_faces`` faces carry lightmaps at ``spacing`` units per
     luxel; the room ceiling (z = 4096) is TRACE_ID_SKY.  Lights: point lights
     with RGB U(50,500), quadratic attenuation, radius 1,024; spotlights with a
-    30/45 degree cone; one sky-ambient light over the 162 sky directions."""
+    30/45 degree cone; one sky-ambient light over the 162 sky directions.
+    ``wall_tiles`` > 1 splits each room face into that many tiles per side
+    (same planes, same lit boxes and lights)."""
     n_boxes = (n_faces + 5) // 6
     soup = TriangleSoup()
-    soup.add_box(TRACE_ID_OPAQUE, (0.0, 0.0, 0.0), (ROOM, ROOM, ROOM),
-                 ceiling_id=TRACE_ID_SKY if sky else None)
+    if wall_tiles > 1:
+        n_room = _tiled_room(soup, wall_tiles, sky)
+    else:
+        soup.add_box(TRACE_ID_OPAQUE, (0.0, 0.0, 0.0), (ROOM, ROOM, ROOM),
+                     ceiling_id=TRACE_ID_SKY if sky else None)
+        n_room = 12
     mins, maxs = _random_boxes(Stream(seed, S_BOXES), n_boxes, *edge)
     faces = []
-    tri_face = [-1] * 12
+    tri_face = [-1] * n_room
     for b in range(n_boxes):
         quads, normals = box_quads(mins[b], maxs[b])
         for k, q in enumerate(quads):
