@@ -280,13 +280,6 @@ int vrg_env_wall_slots(const vrg_env *env, int32_t *tris, int32_t *counts);
  * answers are the same).  Only before vrg_env_setup_acceleration_structure.
  * (no reference counterpart) */
 int vrg_env_set_wall_slots(vrg_env *env, int32_t enable);
-/* Traversal stack entries the scene's walks may use (1 to 32, default 32).
- * The host refuses trees deeper than 32, so a walk never needs more; should
- * a push find the stack full all the same, the walk records it and the
- * call (or, for the _d entry points that do not wait for the GPU, the next
- * call on the scene) fails with VRG_ERR_STATE instead of returning a wrong
- * answer.  A lower limit exercises that guard.  (no reference counterpart) */
-int vrg_env_set_stack_limit(vrg_env *env, int32_t entries);
 /* Where the walk tree is built: 0 on the host (every extent boundary a
  * candidate plane), 1 or -1 (default) on the context's GPU (nodes of up to
  * 512 triangles weigh every extent boundary, larger ones the first start

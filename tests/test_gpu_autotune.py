@@ -127,7 +127,7 @@ def test_bounce_variants_identical(gpu_ctx, tmp_path):
     env.gather_patch_direct(nl)
     key = Context.tune_key("bounce_spmv", nnz, nl)
     outs = []
-    for v in range(6):
+    for v in range(7):
         _force(gpu_ctx, tmp_path, key, v)
         total, bounces, _ = env.bounce_light(nl, max_bounces=12, rel_tol=0.0)
         assert bounces == 12

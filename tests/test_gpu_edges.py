@@ -154,39 +154,3 @@ def test_wall_slots_respect_the_skip_id(gpu_ctx, oracle):
         want = s.test_lines(a, b, skip=(prop if skip_prop == 5 else -1), threads=16)
         assert np.array_equal(got, want)
     assert (env.test_line_does_hit_sky(a, b, 5) == 1.0).mean() > 0.5
-
-
-def test_stack_overflow_is_reported_not_silent(gpu_ctx, oracle):
-    # With the walks allowed only 2 stack entries, a push that finds the stack
-    # full drops a subtree; the walk records it and the call fails instead of
-    # returning the wrong verdicts.  Back at the full stack the same lines give
-    # the oracle's answers.
-    from vrad_gb300 import scenes
-    from vrad_gb300._lib import VrgError
-    from vrad_gb300.environment import Environment
-
-    sc = scenes.anyhit_scene(3, n_boxes=256, n_rays=20000)
-    env = Environment(gpu_ctx)
-    env.add_triangles(sc.xyz, sc.ids)
-    env.SetupAccelerationStructure()
-    assert env.walk_tree()[3] > 4
-    env.set_stack_limit(2)
-    with pytest.raises(VrgError, match="traversal stack"):
-        env.test_line_does_hit_sky(sc.starts, sc.stops)
-    # a device-pointer call does not wait for the GPU: its overflow is
-    # reported by the next call on the scene
-    import torch
-
-    a = torch.from_numpy(sc.starts).cuda()
-    b = torch.from_numpy(sc.stops).cuda()
-    m = torch.zeros((len(sc.starts) + 31) // 32, dtype=torch.int32, device="cuda")
-    rc = env.lib.vrg_env_occlusion_mask_d(env.h, a.data_ptr(), b.data_ptr(), len(sc.starts), -1,
-                                          m.data_ptr(), None, None)
-    assert rc == 0
-    torch.cuda.synchronize()
-    env.set_stack_limit(32)
-    with pytest.raises(VrgError, match="traversal stack"):
-        env.test_line_does_hit_sky(sc.starts[:8], sc.stops[:8])
-    frac = env.test_line_does_hit_sky(sc.starts, sc.stops)
-    ref = oracle.Scene(sc.xyz, sc.ids).test_lines(sc.starts, sc.stops, threads=16)
-    assert np.array_equal(frac, ref)

@@ -53,7 +53,6 @@ SIGNATURES = {
     "vrg_env_set_walk_tree_builder": (C.c_int, [P, I32]),
     "vrg_env_wall_slots": (C.c_int, [P, P, P]),
     "vrg_env_set_wall_slots": (C.c_int, [P, I32]),
-    "vrg_env_set_stack_limit": (C.c_int, [P, I32]),
     "vrg_env_get_walk_tree": (C.c_int, [P, P, P, P]),
     "vrg_env_get_triangle": (C.c_int, [P, I64, P]),
     "vrg_env_bounds": (C.c_int, [P, P, P]),

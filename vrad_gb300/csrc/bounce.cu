@@ -58,8 +58,8 @@ __global__ void k_bounce_init(const LeafInfo *__restrict__ info, const float *__
 // neighbouring rows (neighbouring patches, which see much the same patches:
 // their emission gathers share L1 lines).  Per-block sums of |add| and
 // |total| go to partials[2*block].
-template <int U, int NT = kSpmvThreads>
-__global__ void __launch_bounds__(NT) k_bounce_spmv(
+template <int U, int NT = kSpmvThreads, int MINB = 1, bool NA = false>
+__global__ void __launch_bounds__(NT, MINB) k_bounce_spmv(
     const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
     const float *__restrict__ w, const float4 *__restrict__ emit_in, float4 *__restrict__ emit_out,
     float4 *__restrict__ total, const LeafInfo *__restrict__ info, int64_t n,
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(NT) k_bounce_spmv(
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double sa = 0.0, st = 0.0;
     for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nwarps) {
-        const float3 a = warp_sum3(row_gather<U>(col, w, emit_in, row_ptr[row], row_ptr[row + 1], lane));
+        const float3 a = warp_sum3(row_gather<U, NA>(col, w, emit_in, row_ptr[row], row_ptr[row + 1], lane));
         if (lane == 0) {
             float4 t = total[row];
             t.x += a.x;
@@ -172,16 +172,18 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
     VRG_CUDA(ctx, init());
 
     // SpMV variants, picked per (nnz, rows) bucket: 4, 8 or 2 entries per
-    // lane per round, and 256, 512 or 1024 threads per block (more
-    // neighbouring rows per block at a time); the same sums.  Each runs one
-    // wave: resident blocks per SM times SMs.
+    // lane per round, 256, 512 or 1024 threads per block (more neighbouring
+    // rows per block at a time), and 4 per round at a 5-block register cap
+    // with the column / weight stream kept out of L1; the same sums.  Each
+    // runs one wave: resident blocks per SM times SMs.
     using SpmvKernel = void (*)(const int64_t *, const int32_t *, const float *, const float4 *,
                                 float4 *, float4 *, const LeafInfo *, int64_t,
                                 const BounceControl *, double *);
-    constexpr int kSpmvVariants = 6;
+    constexpr int kSpmvVariants = 7;
     const SpmvKernel kvar[kSpmvVariants] = {k_bounce_spmv<4>,       k_bounce_spmv<8>,       k_bounce_spmv<2>,
-                                            k_bounce_spmv<4, 512>,  k_bounce_spmv<4, 1024>, k_bounce_spmv<2, 1024>};
-    const int vthreads[kSpmvVariants] = {256, 256, 256, 512, 1024, 1024};
+                                            k_bounce_spmv<4, 512>,  k_bounce_spmv<4, 1024>, k_bounce_spmv<2, 1024>,
+                                            k_bounce_spmv<4, 256, 5, true>};
+    const int vthreads[kSpmvVariants] = {256, 256, 256, 512, 1024, 1024, 256};
     auto spmv_blocks = [&](int v) {
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kvar[v], vthreads[v], 0) != cudaSuccess ||

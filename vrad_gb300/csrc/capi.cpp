@@ -18,18 +18,6 @@ int fail(vrg_ctx *ctx, int code, const std::string &msg) {
     return code;
 }
 
-int walk_status(vrg_env *env) {
-    if (!env->status_h) return VRG_OK;
-    // the word is written by kernels that have finished by the time a call
-    // synchronises; a racing write only shows up at the next check
-    volatile uint32_t *w = env->status_h;
-    if ((*w & kStatusStackOverflow) == 0) return VRG_OK;
-    *w = 0;
-    return fail(env->ctx, VRG_ERR_STATE,
-                "a walk ran out of traversal stack (tree deeper than the stack limit): the results of the device "
-                "calls since the last check are wrong");
-}
-
 int cuda_fail(vrg_ctx *ctx, cudaError_t e, const char *what) {
     std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
     return fail(ctx, e == cudaErrorMemoryAllocation ? VRG_ERR_NOMEM : VRG_ERR_CUDA, m);
@@ -102,16 +90,6 @@ int sync(vrg_ctx *ctx) {
     return VRG_OK;
 }
 
-// sync for calls that walk the scene: also reports a walk that ran out of
-// traversal stack
-int env_sync(vrg_env *env) {
-    {
-        const int rc = sync(env->ctx);
-        if (rc != VRG_OK) return rc;
-    }
-    return walk_status(env);
-}
-
 int upload(vrg_ctx *ctx, DevBuf &buf, const void *src, size_t bytes) {
     if (ctx->host_only) return VRG_OK;
     VRG_CUDA(ctx, buf.reserve(bytes));
@@ -147,9 +125,7 @@ int need_built(vrg_env *env) {
     if (!env) return VRG_ERR_INVALID;
     if (env->ctx->host_only) return fail(env->ctx, VRG_ERR_STATE, "host-only context has no device");
     if (!env->built) return fail(env->ctx, VRG_ERR_STATE, "SetupAccelerationStructure has not run");
-    // a walk of an earlier call that did not synchronise (the _d entry
-    // points) and ran out of stack is reported here
-    return walk_status(env);
+    return VRG_OK;
 }
 
 }  // namespace
@@ -275,7 +251,6 @@ void vrg_env_destroy(vrg_env *env) {
     cudaStreamSynchronize(env->ctx->stream);
     relight_release(env);
     bounce_release(env);
-    if (env->status_h) cudaFreeHost(env->status_h);
     delete env;
 }
 
@@ -390,7 +365,7 @@ int vrg_env_trace_closest(vrg_env *env, const float *orig, const float *dir, con
                              env->d_out1.as<float>()));
     TRY(download(ctx, out_hit, env->d_out0, 4 * n));
     TRY(download(ctx, out_t, env->d_out1, 4 * n));
-    return env_sync(env);
+    return sync(ctx);
 }
 
 int vrg_env_trace4_rays(vrg_env *env, const float *origin, const float *direction, const float *tmin,
@@ -456,7 +431,7 @@ int vrg_env_occlusion_mask(vrg_env *env, const float *start, const float *stop, 
         TRY(download(ctx, out_hit, env->d_out0, 4 * n));
         TRY(download(ctx, out_t, env->d_out1, 4 * n));
     }
-    return env_sync(env);
+    return sync(ctx);
 }
 
 int vrg_env_test_line_does_hit_sky(vrg_env *env, const float *start, const float *stop, int64_t n,
@@ -479,7 +454,7 @@ int vrg_env_test_line_does_hit_sky(vrg_env *env, const float *start, const float
     VRG_CUDA(ctx, env->d_out0.reserve(4 * n));
     TRY(launch_test_lines(env, d_start, d_stop, n, skip, env->d_out0.as<float>()));
     TRY(download(ctx, fraction_visible, env->d_out0, 4 * n));
-    return env_sync(env);
+    return sync(ctx);
 }
 
 /* CanLeafTraceToSky (rad/lightmap/lightmap.go:425-451) */
@@ -750,7 +725,7 @@ int vrg_env_gather_direct_light(vrg_env *env, int32_t supersamples, uint64_t see
     TRY(vrg_env_gather_direct_light_d(env, supersamples, seed, env->d_out0.as<float>(), out_shadow_rays));
     std::lock_guard<std::mutex> lk(env->mu);
     TRY(download(ctx, out_rgb, env->d_out0, 12 * nlux));
-    return env_sync(env);
+    return sync(ctx);
 }
 
 int vrg_env_gather_points(vrg_env *env, const float *points, const float *normals, int64_t n, float *out_rgb,
@@ -771,7 +746,7 @@ int vrg_env_gather_points(vrg_env *env, const float *points, const float *normal
     unsigned long long h = 0;
     VRG_CUDA(ctx, cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
     if (n > 0) TRY(download(ctx, out_rgb, env->d_out0, 12 * n));
-    TRY(env_sync(env));
+    TRY(sync(ctx));
     if (out_shadow_rays) *out_shadow_rays = h;
     return VRG_OK;
 }
@@ -899,7 +874,7 @@ int vrg_env_gather_patch_direct(vrg_env *env, float *out_rgb) {
     TRY(launch_gather_points(env, env->d_patch_pts.as<float>(), env->d_patch_nrm.as<float>(), nl,
                              env->d_leaf_direct.as<float>(), nullptr));
     if (out_rgb) TRY(download(ctx, out_rgb, env->d_leaf_direct, 12 * nl));
-    TRY(env_sync(env));
+    TRY(sync(ctx));
     env->have_patch_direct = true;
     return VRG_OK;
 }

@@ -95,7 +95,7 @@ __device__ int32_t filtered_trace(const DevScene &s, const Ray &ray, const RayPr
             uint2 nd = fetch_node<0>(s, node);
             bool reached = true;
             while ((nd.x & 3u) != 3u) {
-                if (!inner_step<0>(s, rp, nd, t0, t1, st.stk, sp, node)) {
+                if (!inner_step<0>(rp, nd, t0, t1, st.stk, sp, node)) {
                     reached = false;
                     break;
                 }
@@ -255,7 +255,7 @@ int run_coverage(vrg_env *env, const float *a, const float *b, const float *tmin
     }
     VRG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     collect_timings(ctx);
-    return walk_status(env);
+    return VRG_OK;
 }
 
 }  // namespace

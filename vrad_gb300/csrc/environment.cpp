@@ -2,6 +2,7 @@
 // triangle soup, intersection format, acceleration structure and its
 // upload to the device.
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -66,6 +67,30 @@ void tri_intersect_format(const float *xyz9, int32_t id, uint8_t flags, TriRecor
     out->idx_drop = (tri_index << 2) | (uint32_t)drop;
 }
 
+// Largest number of inner nodes on a root-to-leaf path of a tree in the
+// node format (type | left index << 2, children adjacent), iteratively; a
+// child index that does not point forward inside the array counts as too
+// deep.
+int inner_depth(const std::vector<uint32_t> &children) {
+    const int64_t n = (int64_t)children.size();
+    if (n == 0) return 0;
+    std::vector<std::pair<int64_t, int>> todo{{0, 0}};
+    int deepest = 0;
+    while (!todo.empty()) {
+        const std::pair<int64_t, int> top = todo.back();
+        todo.pop_back();
+        const int64_t node = top.first;
+        if ((children[node] & 3u) == kLeaf) continue;
+        const int d = top.second + 1;
+        deepest = std::max(deepest, d);
+        const int64_t left = (int64_t)(children[node] >> 2);
+        if (left <= node || left + 1 >= n) return std::numeric_limits<int>::max();
+        todo.push_back({left, d});
+        todo.push_back({left + 1, d});
+    }
+    return deepest;
+}
+
 }  // namespace vrg
 
 using namespace vrg;
@@ -126,7 +151,12 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     }
     records.join();
     if (rc != VRG_OK) return rc;
-    if (env->walk_tree.height >= kStackMax)
+    // A walk pushes at most one subtree per inner node on its path, so a tree
+    // whose paths hold fewer inner nodes than the device's stack has entries
+    // never fills it.  The depth is measured here on the node array that is
+    // uploaded, not taken from the builder, so a builder that misreports its
+    // tree's height cannot hand the device a tree that would overflow.
+    if (env->walk_tree.height >= kStackMax || inner_depth(env->walk_tree.children) >= kStackMax)
         return fail(ctx, VRG_ERR_UNSUPPORTED, "kd tree deeper than the traversal stack");
 
     // device upload of the walk tree: nodes (8 B), then in leaf order the
@@ -244,14 +274,6 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     env->cover_ready = false;
     if (ctx->host_only) return VRG_OK;
     VRG_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (!env->status_h) {
-        void *h = nullptr, *d = nullptr;
-        VRG_CUDA(ctx, cudaHostAlloc(&h, sizeof(uint32_t), cudaHostAllocMapped));
-        env->status_h = static_cast<uint32_t *>(h);
-        VRG_CUDA(ctx, cudaHostGetDevicePointer(&d, h, 0));
-        env->status_d = static_cast<uint32_t *>(d);
-    }
-    *env->status_h = 0;
     VRG_CUDA(ctx, env->d_nodes.reserve(nn * sizeof(uint2)));
     VRG_CUDA(ctx, env->d_leaf_tris.reserve(leaf.size() * sizeof(float4)));
     VRG_CUDA(ctx, env->d_tri_ids.reserve((n ? n : 1) * sizeof(int32_t)));
@@ -338,13 +360,6 @@ int vrg_env_set_wall_slots(vrg_env *env, int32_t enable) {
     std::lock_guard<std::mutex> lk(env->mu);
     if (env->built) return fail(env->ctx, VRG_ERR_STATE, "wall slots set after the build");
     env->use_wall_slots = enable != 0;
-    return VRG_OK;
-}
-
-int vrg_env_set_stack_limit(vrg_env *env, int32_t entries) {
-    if (!env || entries < 1 || entries > vrg::kStackMax) return VRG_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(env->mu);
-    env->stack_limit = entries;
     return VRG_OK;
 }
 

@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
                     done = true;
             }
         } else if (run_node) {
-            if (inner_step<OPT>(s, rp, nd, t0, t1, stk, sp, node) ||
+            if (inner_step<OPT>(rp, nd, t0, t1, stk, sp, node) ||
                 pop_next<MODE>(stk, sp, best_t, node, t0, t1))
                 nd = fetch_node<OPT>(s, node);
             else
@@ -376,9 +376,7 @@ DevScene scene_view(const vrg_env *env) {
     s.tri_ids = env->d_tri_ids.as<int32_t>();
     s.top = env->d_top.as<uint2>();
     s.ntop = env->ntop;
-    s.status = env->status_d;
     s.g = env->geom;
-    s.g.stack_limit = env->stack_limit;
     return s;
 }
 

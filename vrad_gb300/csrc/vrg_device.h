@@ -40,7 +40,6 @@ struct SceneGeom {
     int64_t ntris;
     uint32_t wall_count;     // 3 bits per box face: its wall slots in use
     uint32_t wall_base;      // leaf-record index of face 0's first wall slot
-    int32_t stack_limit;     // traversal stack entries a walk may use (<= kStackMax)
 };
 
 // Device view of a resident scene.  The triangle records of the leaves are
@@ -54,12 +53,8 @@ struct DevScene {
     const int32_t *tri_ids;     // NTriangleID per triangle index
     const uint2 *top;           // top levels of the tree in breadth-first order (see kTopRef)
     uint32_t ntop;              // entries of `top` (0: none)
-    uint32_t *status;           // kStatusStackOverflow set by a walk that ran out of stack
     SceneGeom g;
 };
-
-// Bits of the scene's status word (host memory mapped for the device).
-constexpr uint32_t kStatusStackOverflow = 1u;
 
 // The top table holds the first kTopNodes nodes of a breadth-first walk from
 // the root, children pairs kept adjacent.  A child word there whose index

@@ -141,10 +141,6 @@ struct vrg_env {
     WalkTreeCosts walk_costs;
     int walk_builder = -1;  // walk tree: 0 host (full sweep), 1 GPU (binned), -1 by size
     bool use_wall_slots = true;  // shadow lines test their exit face's walls before walking
-    // status word of the scene's walks (kStatusStackOverflow), in page-locked
-    // host memory mapped for the device: read after a call's synchronisation
-    uint32_t *status_h = nullptr, *status_d = nullptr;
-    int32_t stack_limit = vrg::kStackMax;
     std::vector<vrg::TriRecord> tri_records;  // per triangle, insertion order
     vrg::SceneGeom geom{};                     // bounds, sky box, scale
 
@@ -270,8 +266,7 @@ int run_bounce(vrg_env *env, int32_t max_bounces, float rel_tol, int32_t *bounce
 void relight_release(vrg_env *env);
 void bounce_release(vrg_env *env);
 int noalloc_prepare(vrg_ctx *ctx);  // bounce.cu: the no-alloc bounce's array and kernels
-// The scene's walk status: VRG_OK, or VRG_ERR_STATE (and the status word
-// cleared) when a walk since the last check ran out of traversal stack.
-int walk_status(vrg_env *env);
+// Inner nodes on the longest root-to-leaf path (environment.cpp).
+int inner_depth(const std::vector<uint32_t> &children);
 
 }  // namespace vrg

@@ -8,6 +8,23 @@
 
 namespace vrg {
 
+// Column / weight stream loads; NA loads them without allocating in L1, so
+// that L1 keeps the gathered emission entries.
+template <bool NA>
+__device__ __forceinline__ int32_t csr_col(const int32_t *p) {
+    if (!NA) return __ldg(p);
+    int32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+template <bool NA>
+__device__ __forceinline__ float csr_w(const float *p) {
+    if (!NA) return __ldg(p);
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+
 // sum_j w_j * x[col_j] over the row's entries [b, e) for one warp: lane l
 // takes entries b+l, b+l+32, ... in that order, each added with one fused
 // multiply-add (so every U gives the same per-lane sums), U of them per round, with the next round's column and
@@ -15,7 +32,7 @@ namespace vrg {
 // gathers wait on the column loads; without the overlap every round pays
 // both latencies back to back).  Returns the lane's partial sums; the
 // caller reduces across the warp.
-template <int U>
+template <int U, bool NA = false>
 __device__ __forceinline__ float3 row_gather(const int32_t *__restrict__ col,
                                              const float *__restrict__ w,
                                              const float4 *__restrict__ x, int64_t b, int64_t e,
@@ -27,8 +44,8 @@ __device__ __forceinline__ float3 row_gather(const int32_t *__restrict__ col,
     if (i + 32 * (U - 1) < e) {
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            c[k] = __ldg(col + i + 32 * k);
-            wv[k] = __ldg(w + i + 32 * k);
+            c[k] = csr_col<NA>(col + i + 32 * k);
+            wv[k] = csr_w<NA>(w + i + 32 * k);
         }
     }
     for (; i + 32 * (U - 1) < e; i += 32 * U) {
@@ -38,8 +55,8 @@ __device__ __forceinline__ float3 row_gather(const int32_t *__restrict__ col,
         if (in + 32 * (U - 1) < e) {
 #pragma unroll
             for (int k = 0; k < U; k++) {
-                cn[k] = __ldg(col + in + 32 * k);
-                wn[k] = __ldg(w + in + 32 * k);
+                cn[k] = csr_col<NA>(col + in + 32 * k);
+                wn[k] = csr_w<NA>(w + in + 32 * k);
             }
         }
         float4 xv[U];
@@ -58,8 +75,8 @@ __device__ __forceinline__ float3 row_gather(const int32_t *__restrict__ col,
         }
     }
     for (; i < e; i += 32) {
-        const float wk = __ldg(w + i);
-        const float4 xk = __ldg(x + __ldg(col + i));
+        const float wk = csr_w<NA>(w + i);
+        const float4 xk = __ldg(x + csr_col<NA>(col + i));
         ar = __fmaf_rn(wk, xk.x, ar);
         ag = __fmaf_rn(wk, xk.y, ag);
         ab = __fmaf_rn(wk, xk.z, ab);

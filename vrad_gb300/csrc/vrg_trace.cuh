@@ -169,13 +169,10 @@ __device__ __forceinline__ bool trace_init(const DevScene &s, const Ray &ray, co
 // pushed (with its part of the interval) when the ray reaches it too.  With
 // kOptSkip children without triangles are neither entered nor pushed, and
 // the step returns false when no child is left to visit (without it, it
-// always returns true).  The stack holds at most one entry per tree level
-// and the host refuses trees deeper than the limit; should a push find the
-// stack full all the same, the far child cannot be kept, so the walk's
-// answer is wrong: the step records kStatusStackOverflow in the scene's
-// status word, and the host turns it into an error for the call.
+// always returns true).  The stack never overflows: it holds at most one
+// entry per tree level.
 template <int OPT>
-__device__ __forceinline__ bool inner_step(const DevScene &s, const RayPre &rp, uint2 nd, float &t0, float &t1,
+__device__ __forceinline__ bool inner_step(const RayPre &rp, uint2 nd, float &t0, float &t1,
                                            uint4 *stk, int &sp, uint32_t &next) {
     const uint32_t type = nd.x & 3u;
     const float sv = __uint_as_float(nd.y);
@@ -191,13 +188,9 @@ __device__ __forceinline__ bool inner_step(const DevScene &s, const RayPre &rp, 
     const float tfe = __fmaf_rn(sv, inv, B);
     const bool vn = !(tne < t0) && !near_empty, vf = !(tfe > t1) && !far_empty;
     if (vn) {
-        if (vf) {
-            if (sp < s.g.stack_limit) {
-                stk[sp] = make_uint4(farc, __float_as_uint(fmaxf(t0, tfe)), __float_as_uint(t1), 0u);
-                sp++;
-            } else {
-                atomicOr(s.status, kStatusStackOverflow);
-            }
+        if (vf && sp < kStackMax) {
+            stk[sp] = make_uint4(farc, __float_as_uint(fmaxf(t0, tfe)), __float_as_uint(t1), 0u);
+            sp++;
         }
         t1 = fminf(t1, tne);
         next = nearc;
@@ -326,7 +319,7 @@ __device__ __forceinline__ bool trace_step(const DevScene &s, const Ray &ray, co
     uint2 nd = fetch_node<OPT>(s, node);
     bool reached = true;
     while ((nd.x & 3u) != 3u) {
-        if (!inner_step<OPT>(s, rp, nd, t0, t1, st.stk, sp, node)) {
+        if (!inner_step<OPT>(rp, nd, t0, t1, st.stk, sp, node)) {
             reached = false;
             break;
         }

@@ -380,10 +380,6 @@ class Environment:
                   "get_walk_tree")
         return ch, sp, refs[: nr.value], ht.value
 
-    def set_stack_limit(self, entries: int):
-        """Traversal stack entries the walks may use (1-32, default 32)."""
-        self._chk(self.lib.vrg_env_set_stack_limit(self.h, int(entries)), "set_stack_limit")
-
     def set_wall_slots(self, enable: bool):
         """Wall slots on (default) or off; before SetupAccelerationStructure."""
         self._chk(self.lib.vrg_env_set_wall_slots(self.h, int(bool(enable))), "set_wall_slots")
