@@ -9,8 +9,8 @@ compared luxel by luxel against the oracle (`parity`).
 The same JSON line carries the rest of the metric, one object per workload,
 each with its own error against the oracle and its roofline:
   anyhit     2^20 shadow lines, 12,300 triangles: mask and closest-hit Mrays/s
-  rooms      the headline bake with the wall slots off, and with the room's
-             walls split into 16 x 16 tiles per face: what the slots buy
+  rooms      the headline bake with the wall cells off, and with the room's
+             walls split into 16 x 16 tiles per face: what the cells buy
   radiosity  the same faces at 64-unit patches, 65,536 transfer rays per
              patch: CSR build, bounce SpMV GB/s, solve to 1e-3
   batch      256 scenes baked together vs one scene per launch: bakes/s
@@ -611,11 +611,11 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
 
 
 def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
-    """What the wall slots buy.  The headline's box room has six walls of two
-    triangles each, so most sky lines end on a wall slot test.  Here the same
-    bake runs with the slots off, and on the same scene with each room face
-    split into 16 x 16 tiles (as a map's brush sides make walls: the slots
-    then hold 4 of 512 triangles per face), with and without the slots; the
+    """What the wall cells buy.  The headline's box room has six walls of two
+    triangles each, so most sky lines end on one wall test.  Here the same
+    bake runs with the wall cells off, and on the same scene with each room
+    face split into 16 x 16 tiles (as a map's brush sides make walls: 512
+    triangles per face, one tile per cell), with and without the cells; the
     tiled room's luxels of faces 0-255 are checked against the oracle."""
     import torch
 
@@ -626,8 +626,8 @@ def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
 
     out = {}
     got_tiled = None
-    for name, tiles, slots in (("box_room_slots_off", 1, False), ("tiled_16x16_slots_on", 16, True),
-                               ("tiled_16x16_slots_off", 16, False)):
+    for name, tiles, slots in (("box_room_walls_off", 1, False), ("tiled_16x16_walls_on", 16, True),
+                               ("tiled_16x16_walls_off", 16, False)):
         # a context of its own per room, so that each is autotuned on itself
         ctx = Context(dev.index)
         ctx.set_stream(stream.cuda_stream)
@@ -656,9 +656,9 @@ def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
         tv, tms = ctx.autotune_choice(Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
         out[name] = {"value": round(rays.value / (mean * 1e-3) / 1e6, 1), "unit": "Mrays/s",
                      "ms_per_step": round(mean, 3), "rays_per_step": rays.value,
-                     "triangles": len(lit.ids), "wall_slot_triangles_per_face": env.wall_slots()[1].tolist(),
+                     "triangles": len(lit.ids), "wall_triangles_per_face_reported": env.wall_slots()[1].tolist(),
                      "autotune": {"variant": tv, "variant_ms": [round(x, 3) for x in tms]}}
-        if name == "tiled_16x16_slots_on":
+        if name == "tiled_16x16_walls_on":
             got_tiled = (d_out.cpu().numpy(), lit)
         env.close()
         ctx.close()

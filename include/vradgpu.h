@@ -270,13 +270,19 @@ int vrg_env_get_tree(const vrg_env *env, uint32_t *children, float *split, int32
  * before vrg_env_setup_acceleration_structure. */
 int vrg_env_set_walk_tree_costs(vrg_env *env, float traversal, float intersection,
                                 float empty_bonus, int32_t max_depth);
-/* Wall slots: per face of the scene box (face 2*axis + 1 for a max side),
- * up to 4 opaque triangles lying in that face, largest first (tris[4*face+i],
- * -1 unused).  A shadow line of the direct-light gathers first tests the
- * slots of the face it leaves the box through: a hit before the sky region
- * occludes it whatever lies in between, so the walk is skipped. */
+/* Wall cells: per face of the scene box (face 2*axis + 1 for a max side),
+ * the opaque triangles lying in that face (a room's walls and floor, or the
+ * brush sides a map's walls are made of): up to 4 per face in fixed slots
+ * when no face has more, otherwise a grid over each face whose cells list
+ * the triangles overlapping them.  A shadow line of the gathers first tests
+ * the slots or the cell of the face through which it leaves the box: a hit
+ * before the sky region occludes it whatever lies in between, so the walk
+ * is skipped.
+ * This call reports, per face, the number of such triangles (at most 4
+ * counted) and the first 4, largest first (tris[4*face+i], -1 unused).
+ * (no reference counterpart) */
 int vrg_env_wall_slots(const vrg_env *env, int32_t *tris, int32_t *counts);
-/* Wall slots on (1, the default) or off (0: every line is walked; the
+/* Wall cells on (1, the default) or off (0: every line is walked; the
  * answers are the same).  Only before vrg_env_setup_acceleration_structure.
  * (no reference counterpart) */
 int vrg_env_set_wall_slots(vrg_env *env, int32_t enable);

@@ -28,8 +28,8 @@ constexpr int kThreads = 128;
 // bake, which alone are too few to fill the GPU.
 // TILE walks each face's luxels in 4 x 2 tiles (tile_luxel) instead of row
 // order; the output is the same, each luxel written by the lane holding its
-// first sample.
-template <int FETCH, int OPT = 0, bool TILE = false>
+// first sample.  WM is the scene's wall layout (slots or cells).
+template <int FETCH, int OPT = 0, bool TILE = false, int WM = kWallSlotsOnly>
 __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
             ny = fr.normal.y;
             nz = fr.normal.z;
         }
-        if (gi < total) gather_point<kSkyTrace, OPT>(s, lights, nl, px, py, pz, nx, ny, nz, r, g, b, rays);
+        if (gi < total) gather_point<kSkyTrace, OPT, WM>(s, lights, nl, px, py, pz, nx, ny, nz, r, g, b, rays);
         if (is_pt) {
             const int64_t i = gi - nsamp;
             pout[3 * i] = r;
@@ -160,6 +160,34 @@ void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst) {
     }
 }
 
+// The seven tuned variants of k_direct_luxels for wall layout WM: samples
+// claimed per warp (32, 64, 128), 32 with the leaf records kept out of L1,
+// 32 in 4 x 2 luxel tiles without and with the top of the tree in shared
+// memory, and in tiles skipping children without triangles.
+template <int WM>
+void launch_direct_variant(int v, int grid, cudaStream_t st, const DevScene &s, const DevLight *lights, int nl,
+                           const vrg_env *env, int64_t nlux, int ss, uint64_t seed, float *out_rgb,
+                           const float *pts, const float *nrm, int64_t npts, float *pts_out,
+                           unsigned long long *d_rays, unsigned long long *work) {
+    const FaceRec *faces = env->d_faces.as<FaceRec>();
+    const int64_t *off = env->d_luxel_offset.as<int64_t>();
+    const int nf = env->nfaces;
+    if (v == 0)
+        k_direct_luxels<32, 0, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else if (v == 1)
+        k_direct_luxels<64, 0, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else if (v == 2)
+        k_direct_luxels<128, 0, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else if (v == 3)
+        k_direct_luxels<32, kOptStream, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else if (v == 4)
+        k_direct_luxels<32, 0, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else if (v == 5)
+        k_direct_luxels<32, kOptTop, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else
+        k_direct_luxels<32, kOptSkip, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+}
+
 int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
                          unsigned long long *d_rays, const float *pts, const float *nrm, int64_t npts,
                          float *pts_out) {
@@ -177,30 +205,20 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     const DevScene s = scene_view(env);
     const DevLight *lights = env->d_lights.as<DevLight>();
     const int nl = (int)env->lights.size();
-    // variants: samples claimed per warp (32, 64, 128), 32 with the leaf
-    // records kept out of L1, 32 in 4 x 2 luxel tiles without and with the
-    // top of the tree in shared memory, and in tiles skipping children
-    // without triangles; picked per bucket
+    // the variants of launch_direct_variant, picked per bucket, built for the
+    // scene's wall layout
     auto launch = [&](int v) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(work, 0, 8, ctx->stream);
         if (e == cudaSuccess && d_rays) e = cudaMemsetAsync(d_rays, 0, 8, ctx->stream);
         if (e != cudaSuccess) return e;
         cudaEvent_t ev = nullptr;
         timing_begin(ctx, "direct_luxels", &ev);
-        if (v == 0)
-            k_direct_luxels<32><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else if (v == 1)
-            k_direct_luxels<64><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else if (v == 2)
-            k_direct_luxels<128><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else if (v == 3)
-            k_direct_luxels<32, kOptStream><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else if (v == 4)
-            k_direct_luxels<32, 0, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-        else if (v == 5)
-            k_direct_luxels<32, kOptTop, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+        if (env->wall_layout == 0)
+            launch_direct_variant<kWallSlotsOnly>(v, grid, ctx->stream, s, lights, nl, env, nlux, ss, seed, out_rgb,
+                                                  pts, nrm, npts, pts_out, d_rays, work);
         else
-            k_direct_luxels<32, kOptSkip, true><<<grid, kThreads, 0, ctx->stream>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(), env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+            launch_direct_variant<kWallCellsOnly>(v, grid, ctx->stream, s, lights, nl, env, nlux, ss, seed, out_rgb,
+                                                  pts, nrm, npts, pts_out, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;

@@ -209,11 +209,18 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
         }
     }
     env->ntop = (uint32_t)top.size();
-    // wall slots: per face of the scene box, the largest opaque triangles
-    // lying in that face (a closed room's walls and floor), appended after
-    // the leaf entries so that a shadow line can test the face it leaves
-    // through before walking
+    // walls: per face of the scene box, the opaque triangles lying in that
+    // face (a closed room's walls and floor, or the brush sides a map's walls
+    // are made of), as extra leaf records after the leaf entries: in the
+    // face's slots when no face has more than kWallSlots of them, otherwise
+    // behind a grid over each face whose cells list the triangles whose
+    // extent overlaps them, largest first, at most kWallCellMax.  A shadow
+    // line tests the slots or the cell of the face it leaves the box through
+    // before walking
+    // (wall_occludes).  The first kWallSlots triangles of each face are
+    // what vrg_env_wall_slots reports.
     std::vector<int32_t> wall[6];
+    std::vector<double> wall_area[6];
     {
         std::vector<std::pair<double, int32_t>> cand[6];
         for (int64_t t = 0; t < (env->use_wall_slots ? n : 0); t++) {
@@ -234,11 +241,25 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
                 }
         }
         for (int f = 0; f < 6; f++) {
-            std::sort(cand[f].begin(), cand[f].end());
-            for (size_t i = 0; i < cand[f].size() && (int)i < kWallSlots; i++) wall[f].push_back(cand[f][i].second);
+            std::stable_sort(cand[f].begin(), cand[f].end());
+            for (const auto &c : cand[f]) {
+                wall[f].push_back(c.second);
+                wall_area[f].push_back(-c.first);
+            }
         }
     }
-    const size_t ne = nr + 6 * (size_t)kWallSlots;  // leaf entries + wall slots
+    // one layout per scene, so that the direct-light kernel can be built for
+    // it alone: a scene whose faces have at most kWallSlots triangles each (a
+    // box room's walls) keeps them in the slots at fixed records
+    // nr + kWallSlots * f + i, tested without a table; otherwise every face
+    // that has any gets a cell grid over records after the slots
+    bool use_cells = false;
+    for (int f = 0; f < 6; f++) use_cells = use_cells || wall[f].size() > (size_t)kWallSlots;
+    env->wall_layout = use_cells ? 1 : 0;
+    size_t nw = 6 * (size_t)kWallSlots;
+    for (int f = 0; f < 6; f++)
+        if (use_cells) nw += wall[f].size();
+    const size_t ne = nr + nw;  // leaf entries + wall slots + wall-cell records
     std::vector<float4> leaf(3 * ne, make_float4(0, 0, 0, 0));
     auto put = [&](size_t r, int32_t tri) {
         const TriRecord &t = env->tri_records[tri];
@@ -252,12 +273,78 @@ int vrg_env_setup_acceleration_structure(vrg_env *env) {
     };
     g.wall_base = (uint32_t)nr;
     g.wall_count = 0;
+    g.wall_cell_mask = 0;
+    env->n_wall_records = nw;
+    // the cell table: 6 face descriptors of kWallFaceWords words (cell origin
+    // and inverse size in the face's two in-plane axes as float bits, cells
+    // per axis, offset of the face's cell starts), then per face with walls
+    // gu * gv + 1 cell starts (indices into this table) and the entries
+    // (leaf-record indices)
+    std::vector<uint32_t> &cells = env->wall_cells;
+    cells.assign(6 * kWallFaceWords, 0u);
+    size_t rec = nr + 6 * (size_t)kWallSlots;
     for (int f = 0; f < 6; f++) {
         for (int i = 0; i < kWallSlots; i++)
             env->wall_tris[kWallSlots * f + i] = i < (int)wall[f].size() ? wall[f][i] : -1;
-        env->wall_counts[f] = (int32_t)wall[f].size();
-        for (size_t i = 0; i < wall[f].size(); i++) put(nr + (size_t)kWallSlots * f + i, wall[f][i]);
-        g.wall_count |= (uint32_t)wall[f].size() << (3 * f);
+        env->wall_counts[f] = (int32_t)std::min<size_t>(wall[f].size(), kWallSlots);
+        const size_t nf = wall[f].size();
+        if (nf == 0) continue;
+        if (!use_cells) {
+            for (size_t i = 0; i < nf; i++) put(nr + (size_t)kWallSlots * f + i, wall[f][i]);
+            g.wall_count |= (uint32_t)nf << (3 * f);
+            continue;
+        }
+        const int a = f >> 1, au = (a + 1) % 3, av = (a + 2) % 3;
+        const int gs = std::max(1, std::min(kWallGridMax, (int)std::ceil(std::sqrt((double)nf / 2.0))));
+        const float u0 = env->min_bound[au], v0 = env->min_bound[av];
+        const float du = (env->max_bound[au] - u0) / (float)gs, dv = (env->max_bound[av] - v0) / (float)gs;
+        const int gu = du > 0.0f ? gs : 1, gv = dv > 0.0f ? gs : 1;
+        const float iu = du > 0.0f ? 1.0f / du : 0.0f, iv = dv > 0.0f ? 1.0f / dv : 0.0f;
+        std::vector<std::vector<uint32_t>> cl((size_t)gu * gv);
+        for (size_t i = 0; i < nf; i++, rec++) {
+            put(rec, wall[f][i]);
+            const float *v = &env->xyz[9 * (size_t)wall[f][i]];
+            const float umin = std::min(v[au], std::min(v[3 + au], v[6 + au]));
+            const float umax = std::max(v[au], std::max(v[3 + au], v[6 + au]));
+            const float vmin = std::min(v[av], std::min(v[3 + av], v[6 + av]));
+            const float vmax = std::max(v[av], std::max(v[3 + av], v[6 + av]));
+            // the cells the triangle's extent overlaps (an extent ending on a
+            // cell edge does not reach into the next cell)
+            auto span = [](float lo, float hi, float x0, float inv, int g, int &c0, int &c1) {
+                const float a = (lo - x0) * inv, b = (hi - x0) * inv;
+                c0 = (int)std::min((float)(g - 1), std::max(0.0f, std::floor(a)));
+                c1 = (int)std::min((float)(g - 1), std::max((float)c0, std::ceil(b) - 1.0f));
+            };
+            int c0, c1, r0, r1;
+            span(umin, umax, u0, iu, gu, c0, c1);
+            span(vmin, vmax, v0, iv, gv, r0, r1);
+            for (int cu = c0; cu <= c1; cu++)
+                for (int cv = r0; cv <= r1; cv++)
+                    if (cl[(size_t)cu * gv + cv].size() < (size_t)kWallCellMax)
+                        cl[(size_t)cu * gv + cv].push_back((uint32_t)rec);
+        }
+        uint32_t *d = &cells[(size_t)f * kWallFaceWords];
+        memcpy(&d[0], &u0, 4);
+        memcpy(&d[1], &v0, 4);
+        memcpy(&d[2], &iu, 4);
+        memcpy(&d[3], &iv, 4);
+        d[4] = (uint32_t)gu;
+        d[5] = (uint32_t)gv;
+        d[6] = (uint32_t)cells.size();
+        const size_t starts = cells.size();
+        cells.resize(starts + (size_t)gu * gv + 1);
+        for (size_t c = 0; c < cl.size(); c++) {
+            cells[starts + c] = (uint32_t)cells.size();
+            cells.insert(cells.end(), cl[c].begin(), cl[c].end());
+        }
+        cells[starts + cl.size()] = (uint32_t)cells.size();
+        g.wall_cell_mask |= 1u << f;
+    }
+    {  // the cell table after the edge part (wall_table), padded to whole float4s
+        cells.resize((cells.size() + 3) & ~(size_t)3, 0u);
+        const size_t at = leaf.size();
+        leaf.resize(at + cells.size() / 4);
+        memcpy(&leaf[at], cells.data(), cells.size() * sizeof(uint32_t));
     }
     {  // the leaf entries, in parallel chunks
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));

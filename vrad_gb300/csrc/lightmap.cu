@@ -61,27 +61,28 @@ __device__ __forceinline__ uint32_t encode_sample(float r, float g, float b) {
            ((uint32_t)(uint8_t)(int8_t)x << 24);
 }
 
-// One warp per face, faces taken in order from a work counter (zeroed
-// before the launch), so that a 16-luxel face does not hold a whole block
-// and blocks that draw large faces do not set the tail: the lanes read the
-// face record (one broadcast) and take its luxels in order (coalesced
-// 12-byte reads and 4-byte writes), and the face's patch-tree nodes stay in
-// L1 while its luxels descend them.  No luxel -> face search.
+// One block per face, faces taken in order from a work counter (zeroed
+// before the launch), so that the blocks that draw large faces do not set
+// the tail as a static stride over faces did: every thread reads the same
+// face record (one broadcast), the threads take the face's luxels in order
+// (coalesced 12-byte reads and 4-byte writes), and the face's patch-tree
+// nodes stay in L1 while its luxels descend them.  No luxel -> face search.
 __global__ void __launch_bounds__(kThreads) k_lightmap(
     const FaceRec *__restrict__ faces, const int64_t *__restrict__ off, int nfaces,
     const float *__restrict__ rgb, const float4 *__restrict__ total, const PatchNode *__restrict__ pnodes,
     const int32_t *__restrict__ face_root, uint32_t *__restrict__ out, unsigned int *__restrict__ work) {
-    const int lane = threadIdx.x & 31;
+    __shared__ int face_sh;
     for (;;) {
-        int f = 0;
-        if (lane == 0) f = (int)atomicAdd(work, 1u);
-        f = __shfl_sync(0xffffffffu, f, 0);
+        __syncthreads();  // every thread has read the previous face number
+        if (threadIdx.x == 0) face_sh = (int)atomicAdd(work, 1u);
+        __syncthreads();
+        const int f = face_sh;
         if (f >= nfaces) break;
         const FaceRec fr = faces[f];
         const int64_t base = __ldg(off + f);
         const int64_t n = __ldg(off + f + 1) - base;
         const int32_t root = __ldg(face_root + f);
-        for (int64_t local = lane; local < n; local += 32) {
+        for (int64_t local = threadIdx.x; local < n; local += blockDim.x) {
             const int64_t lux = base + local;
             const int iv = (int)(local / fr.nu);
             const int iu = (int)(local - (int64_t)iv * fr.nu);
@@ -126,8 +127,7 @@ int vrg_env_get_lightmap(vrg_env *env, uint8_t *samples, int64_t *face_offset) {
     // words the gathers use
     unsigned int *work = reinterpret_cast<unsigned int *>(env->d_work.as<char>() + 128);
     VRG_CUDA(ctx, cudaMemsetAsync(work, 0, sizeof(unsigned int), st));
-    const int grid = (int)std::min<int64_t>((env->nfaces + kThreads / 32 - 1) / (kThreads / 32),
-                                            (int64_t)ctx->num_sms * 16);
+    const int grid = (int)std::min<int64_t>(env->nfaces, (int64_t)ctx->num_sms * 16);
     cudaEvent_t ev = nullptr;
     timing_begin(ctx, "lightmap", &ev);
     k_lightmap<<<grid, kThreads, 0, st>>>(env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(),

@@ -372,7 +372,7 @@ DevScene scene_view(const vrg_env *env) {
     DevScene s;
     s.nodes = env->d_nodes.as<uint2>();
     s.leaf_planes = env->d_leaf_tris.as<float4>();
-    s.leaf_edges = s.leaf_planes + env->walk_tree.refs.size() + 6 * (size_t)kWallSlots;
+    s.leaf_edges = s.leaf_planes + env->walk_tree.refs.size() + env->n_wall_records;
     s.tri_ids = env->d_tri_ids.as<int32_t>();
     s.top = env->d_top.as<uint2>();
     s.ntop = env->ntop;

@@ -28,9 +28,22 @@ struct alignas(16) TriRecord {
 };
 static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
 
-// Wall slots: per face of the scene box (2 * axis + 1 for the max side), up
-// to kWallSlots opaque triangles lying in that face, as extra leaf records.
+// Walls: per face of the scene box (2 * axis + 1 for the max side), the
+// opaque triangles lying in that face as extra leaf records.  A face of at
+// most kWallSlots of them keeps them in its slots (records wall_base +
+// kWallSlots * face + i); a larger one gets a grid of at most kWallGridMax x
+// kWallGridMax cells over the face, each listing at most kWallCellMax of the
+// triangles that overlap it.  The cell table is one
+// uint32 array: 6 face descriptors of kWallFaceWords words -- cell origin in
+// the face's in-plane axes (a+1)%3, (a+2)%3 and inverse cell size (float
+// bits), cells per axis, the table index of the face's cell starts -- then,
+// per face with walls, gu * gv + 1 cell starts (table indices) followed by
+// the cells' entries (leaf-record indices).  vrg_env_wall_slots reports the
+// first kWallSlots triangles of each face.
 constexpr int kWallSlots = 4;
+constexpr int kWallGridMax = 32;
+constexpr int kWallCellMax = 8;
+constexpr int kWallFaceWords = 8;
 
 struct SceneGeom {
     float bmin[3], bmax[3];  // root bounds (CalculateTriangleListBounds)
@@ -40,12 +53,17 @@ struct SceneGeom {
     int64_t ntris;
     uint32_t wall_count;     // 3 bits per box face: its wall slots in use
     uint32_t wall_base;      // leaf-record index of face 0's first wall slot
+    uint32_t wall_cell_mask; // bit f set: box face f has a wall-cell grid
 };
 
 // Device view of a resident scene.  The triangle records of the leaves are
 // split in two arrays indexed by TriangleIndexList position: the plane
 // (Nx, Ny, Nz, D), which the test reads first and which rejects most
 // triangles, and the edge part (e0..e3), (e4, e5, id, index<<2 | drop).
+// The entries are the tree's, then the walls' records; the wall-cell table
+// follows the edge part in the same buffer (wall_table).  It has no pointer
+// of its own: one more pointer in this kernel argument changed the
+// direct-light kernel's register allocation and cost it 5 %.
 struct DevScene {
     const uint2 *nodes;         // (children, split bits) per kd node
     const float4 *leaf_planes;  // 1 float4 per TriangleIndexList entry
@@ -55,6 +73,12 @@ struct DevScene {
     uint32_t ntop;              // entries of `top` (0: none)
     SceneGeom g;
 };
+
+// The wall-cell table (see kWallFaceWords), right after the edge part:
+// leaf_edges - leaf_planes records, 2 float4 each.
+__host__ __device__ inline const uint32_t *wall_table(const DevScene &s) {
+    return reinterpret_cast<const uint32_t *>(s.leaf_edges + 2 * (s.leaf_edges - s.leaf_planes));
+}
 
 // The top table holds the first kTopNodes nodes of a breadth-first walk from
 // the root, children pairs kept adjacent.  A child word there whose index

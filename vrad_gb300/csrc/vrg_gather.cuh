@@ -53,7 +53,7 @@ __device__ __forceinline__ uint64_t splitmix(uint64_t seed, uint64_t i) {
 // gather with the edited table.
 enum SkyMode { kSkyTrace = 0, kSkyWrite = 1, kSkyRead = 2 };
 
-template <int SKY, int OPT = 0>
+template <int SKY, int OPT = 0, int WM = kWallAny>
 static __device__ void gather_point(const DevScene &s, const DevLight *__restrict__ lights, int nl,
                                     float px, float py, float pz, float nx, float ny, float nz,
                                     float &r, float &g, float &b, uint32_t &rays,
@@ -105,7 +105,7 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
                 occ = !(vis[li >> 5] & bit);
             } else {
                 rays++;
-                occ = line_occluded<OPT>(s, make_line(px, py, pz, lo.x, lo.y, lo.z), -1);
+                occ = line_occluded<OPT, WM>(s, make_line(px, py, pz, lo.x, lo.y, lo.z), -1);
                 if (SKY != kSkyTrace && vis) {
                     if (occ) vis[li >> 5] &= ~bit;
                     else vis[li >> 5] |= bit;
@@ -129,7 +129,7 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
                     const Line L = make_line(px, py, pz, radd(px, rmul(dx, kMaxTraceLength)),
                                              radd(py, rmul(dy, kMaxTraceLength)),
                                              radd(pz, rmul(dz, kMaxTraceLength)));
-                    if (!line_occluded<OPT>(s, L, -1)) m = cosr;
+                    if (!line_occluded<OPT, WM>(s, L, -1)) m = cosr;
                 }
             } else {
                 float sw = 0.0f, sv = 0.0f;
@@ -142,7 +142,7 @@ static __device__ void gather_point(const DevScene &s, const DevLight *__restric
                     const Line L = make_line(px, py, pz, radd(px, rmul(ax, kMaxTraceLength)),
                                              radd(py, rmul(ay, kMaxTraceLength)),
                                              radd(pz, rmul(az, kMaxTraceLength)));
-                    if (!line_occluded<OPT>(s, L, -1)) sv = radd(sv, w);
+                    if (!line_occluded<OPT, WM>(s, L, -1)) sv = radd(sv, w);
                 }
                 if (sw > 0.0f) m = rdiv(sv, sw);
             }

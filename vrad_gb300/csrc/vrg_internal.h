@@ -138,6 +138,9 @@ struct vrg_env {
     HostTree walk_tree;   // the tree the device walks (build_walk_tree)
     int32_t wall_tris[6 * vrg::kWallSlots];  // wall slots per scene-box face (-1: unused)
     int32_t wall_counts[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<uint32_t> wall_cells;  // the wall-cell table (see vrg_device.h)
+    size_t n_wall_records = 0;          // wall triangles' leaf records after the leaf entries
+    int wall_layout = 0;                // 0: wall slots, 1: wall cells (see vrg_device.h)
     WalkTreeCosts walk_costs;
     int walk_builder = -1;  // walk tree: 0 host (full sweep), 1 GPU (binned), -1 by size
     bool use_wall_slots = true;  // shadow lines test their exit face's walls before walking
