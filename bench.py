@@ -293,16 +293,23 @@ def _event_ms(stream, fn, steps, flush):
 
 
 def _trace_roofline(kernel, units, avg_ms, bytes_per_unit, hbm_peak, hbm_kind, l2, clk, sms,
-                    prof, bytes_model, nodes, tris):
+                    prof, bytes_model, nodes, tris, variant=None):
     """Roofline record of a traversal kernel.  Its algorithmic bytes (kd
     nodes and leaf records) are served from L1 and L2, so the governing roof
     is instruction issue; the L2 and HBM fractions are given beside it, HBM
-    from the DRAM bytes ncu counted for the same kernel."""
+    from the DRAM bytes ncu counted for the same kernel.  The instruction
+    count is the tuned variant's own (`warp_instructions_per_unit_v<n>`)
+    where the summary has it."""
     alg = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
     traffic = _ncu_traffic(prof)
     sm_mhz = (clk or {}).get("sm_mhz")
-    issue = issue_roofline(_profile_value(prof, "warp_instructions_per_unit"), units, avg_ms,
-                           sm_mhz, sms, f"profiles/{prof}")
+    inst = _profile_value(prof, f"warp_instructions_per_unit_v{variant}") if variant is not None else None
+    inst_of = f"variant {variant}" if inst is not None else "the variant the summary names"
+    if inst is None:
+        inst = _profile_value(prof, "warp_instructions_per_unit")
+    issue = issue_roofline(inst, units, avg_ms, sm_mhz, sms, f"profiles/{prof}")
+    if issue:
+        issue["instructions_of"] = inst_of
     rec = {"bound": "issue", "kernel": kernel, "kernel_ms": round(avg_ms, 4),
            "bytes_per_unit": round(bytes_per_unit, 2), "bytes_model": bytes_model,
            "nodes_per_unit": round(float(nodes), 3), "tris_per_unit": round(float(tris), 3),
@@ -462,7 +469,7 @@ def run_gpu(args, rank, world, local_rank):
         f"ncu_{kernel}.txt",
         "8 per kd node + 48 per triangle test (leaf-ordered records and wall slots), means of "
         "the oracle's walk of the device's tree, with the device's options and wall test, over "
-        "the lines of faces 0-255, + sample position, normal and RGB share", nodes, tris)
+        "the lines of faces 0-255, + sample position, normal and RGB share", nodes, tris, tv)
     line = {
         "metric": "shadow Mrays/s (direct-light gather)",
         "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -570,13 +577,13 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
     tv, tms = lib_ctx.autotune_choice(Context.tune_key("trace_mask", env.num_triangles(), n))
     hv, hms = lib_ctx.autotune_choice(Context.tune_key("trace_mask_hit", env.num_triangles(), n))
     # the device's walk, counted by the oracle on the device's tree
-    skip_empty = tv in (12, 13, 14, 15)
+    skip_empty = tv in (12, 13, 14, 15, 16, 17)
     s.set_tree(*env.walk_tree()[:3])
     s.set_skip_empty(skip_empty)
     _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
     nodes, tris = st[:, 0].mean(), st[:, 1].mean()
     bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
-    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15) else (
+    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15, 16, 17) else (
         "ncu_trace_unit_stream.txt" if tv in (6, 7, 9, 10, 11) else "ncu_trace_mask.txt")
     peak, kind = _peaks()
     avg_ms = kms / max(kn, 1)
@@ -603,7 +610,7 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
         "roofline": _trace_roofline(
             "trace_mask", n, avg_ms, bytes_per_unit, peak, kind, l2, clk, sms, prof,
             "24 end points + 1/8 mask + 8 per kd node + 48 per triangle test, means of the "
-            "oracle's walk of the device's tree with the device's options", nodes, tris),
+            "oracle's walk of the device's tree with the device's options", nodes, tris, tv),
         "cpu_baseline": {"value": round(n / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads,
                          "kind": "port", "sample": f"all {n} lines, the reference's SAH tree"},
         "clocks": clk,
@@ -613,10 +620,13 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
 def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
     """What the wall cells buy.  The headline's box room has six walls of two
     triangles each, so most sky lines end on one wall test.  Here the same
-    bake runs with the wall cells off, and on the same scene with each room
-    face split into 16 x 16 tiles (as a map's brush sides make walls: 512
-    triangles per face, one tile per cell), with and without the cells; the
-    tiled room's luxels of faces 0-255 are checked against the oracle."""
+    bake runs with the wall cells off; on the same scene with each room face
+    split into 16 x 16 tiles (512 triangles per face, one tile per cell);
+    and on the same boxes, faces and lights written as a compiled map's
+    brushes (16-unit thick walls, a sky face over the room) and ingested
+    through add_bsp_world (addBrushesForRayTrace) -- each with and without
+    the cells.  The tiled room's and the brush world's luxels of faces 0-255
+    are checked against the oracle."""
     import torch
 
     from vrad_gb300 import scenes
@@ -625,17 +635,22 @@ def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
     from vrad_gb300.environment import Context
 
     out = {}
-    got_tiled = None
+    checked = {}
     for name, tiles, slots in (("box_room_walls_off", 1, False), ("tiled_16x16_walls_on", 16, True),
-                               ("tiled_16x16_walls_off", 16, False)):
+                               ("tiled_16x16_walls_off", 16, False), ("brush_world_walls_on", 0, True),
+                               ("brush_world_walls_off", 0, False)):
         # a context of its own per room, so that each is autotuned on itself
         ctx = Context(dev.index)
         ctx.set_stream(stream.cuda_stream)
         lib = ctx.lib
-        lit = scenes.lit_scene(SEED, wall_tiles=tiles)
         env = Environment(ctx)
         env.set_wall_slots(slots)
-        env.add_triangles(lit.xyz, lit.ids)
+        if tiles == 0:
+            lumps, lit = scenes.lit_brush_world(SEED)
+            env.add_bsp_world(lumps)
+        else:
+            lit = scenes.lit_scene(SEED, wall_tiles=tiles)
+            env.add_triangles(lit.xyz, lit.ids)
         env.SetupAccelerationStructure()
         env.set_faces(lit)
         env.set_lights(lit.lights)
@@ -656,21 +671,22 @@ def sub_rooms(args, lib_ctx, stream, dev, flush, l2, sms):
         tv, tms = ctx.autotune_choice(Context.tune_key("direct_luxels", env.num_triangles(), nlux * 4))
         out[name] = {"value": round(rays.value / (mean * 1e-3) / 1e6, 1), "unit": "Mrays/s",
                      "ms_per_step": round(mean, 3), "rays_per_step": rays.value,
-                     "triangles": len(lit.ids), "wall_triangles_per_face_reported": env.wall_slots()[1].tolist(),
+                     "triangles": env.num_triangles(),
+                     "wall_triangles_per_face_reported": env.wall_slots()[1].tolist(),
                      "autotune": {"variant": tv, "variant_ms": [round(x, 3) for x in tms]}}
-        if name == "tiled_16x16_walls_on":
-            got_tiled = (d_out.cpu().numpy(), lit)
+        if slots and name != "box_room_walls_off":
+            checked[name.replace("_walls_on", "")] = (d_out.cpu().numpy(), lit, *env.get_triangle_vertices())
         env.close()
         ctx.close()
     from oracle import pyoracle
 
-    got, lit = got_tiled
-    off = lit.luxel_offset()
-    nf = min(256, lit.n_faces)
-    ref, _ = pyoracle.gather_luxels(pyoracle.Scene(lit.xyz, lit.ids), pyoracle.make_lights(lit.lights),
-                                    len(lit.lights), lit, 0, nf, ss=4, seed=SEED,
-                                    threads=os.cpu_count() or 1)
-    out["tiled_parity_faces_0_255"] = rel_error_stats(got[: off[nf]], ref)
+    for key, (got, lit, xyz, ids) in checked.items():
+        off = lit.luxel_offset()
+        nf = min(256, lit.n_faces)
+        ref, _ = pyoracle.gather_luxels(pyoracle.Scene(xyz, ids), pyoracle.make_lights(lit.lights),
+                                        len(lit.lights), lit, 0, nf, ss=4, seed=SEED,
+                                        threads=os.cpu_count() or 1)
+        out[f"{key}_parity_faces_0_255"] = rel_error_stats(got[: off[nf]], ref)
     return out
 
 

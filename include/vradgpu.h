@@ -137,7 +137,8 @@ int vrg_ctx_set_autotune(vrg_ctx *ctx, int enable);
 /* The variant chosen for `key` (-1 if untuned) and, when `ms` is not NULL,
  * up to `cap` per-variant times of the tuning run. */
 int vrg_ctx_autotune_choice(vrg_ctx *ctx, const char *key, int32_t *variant, double *ms, int32_t cap);
-/* Save / load the tuned choices as text lines "key variant". */
+/* Save / load the tuned choices as text lines "key variant" (a launch site
+ * has at most 32 variants; a line naming another number is ignored). */
 int vrg_ctx_autotune_save(vrg_ctx *ctx, const char *path);
 int vrg_ctx_autotune_load(vrg_ctx *ctx, const char *path);
 

@@ -12,73 +12,7 @@ SKY, OPAQUE = 0x01000000, 0x02000000
 SURF_SKY, CONTENTS_SOLID, CONTENTS_WATER = 0x4, 0x1, 0x20
 
 
-class World:
-    """Lump arrays of a small compiled map, written the way a BSP lays them out:
-    planes in pairs (p ^ 1 faces the other way), brushes over brush sides,
-    leaves over leaf brushes, faces over signed surfedges."""
-
-    def __init__(self):
-        self.planes, self.sides, self.brushes = [], [], []
-        self.texinfo = [0, SURF_SKY]  # texinfo 0 plain, 1 sky
-        self.verts, self.edges, self.surf, self.faces = [], [[0, 0]], [], []
-
-    def plane(self, n, d):
-        n = np.asarray(n, np.float32)
-        self.planes += [[*n, d], [*(-n), -d]]
-        return len(self.planes) - 2
-
-    def brush(self, planes, contents=CONTENTS_SOLID, texinfo=None, disp=None, bevel=None):
-        first = len(self.sides)
-        for i, (n, d) in enumerate(planes):
-            self.sides.append([self.plane(n, d), (texinfo or {}).get(i, 0), (disp or {}).get(i, 0),
-                               (bevel or {}).get(i, 0)])
-        self.brushes.append([first, len(planes), contents])
-        return len(self.brushes) - 1
-
-    def box(self, mn, mx, **kw):
-        planes = []
-        for a in range(3):
-            e = np.zeros(3, np.float32)
-            e[a] = 1
-            planes += [(e, float(mx[a])), (-e, -float(mn[a]))]
-        return self.brush(planes, **kw)
-
-    def face(self, pts, texinfo=1, flip_every=2):
-        first = len(self.surf)
-        base = len(self.verts)
-        self.verts += [list(p) for p in pts]
-        n = len(pts)
-        for j in range(n):
-            a, b = base + j, base + (j + 1) % n
-            if j % flip_every == 1:  # stored the other way round: read through -edge
-                self.edges.append([b, a])
-                self.surf.append(-(len(self.edges) - 1))
-            else:
-                self.edges.append([a, b])
-                self.surf.append(len(self.edges) - 1)
-        self.faces.append([first, n, texinfo])
-
-    def lumps(self, leaves=None):
-        """leaves: brush lists of the leaves, which a chain of nodes visits in
-        order (node k: leaf k in front, node k + 1 behind; the last node has
-        the last two leaves; one leaf sits on both sides of node 0)."""
-        leaves = leaves if leaves is not None else [list(range(len(self.brushes)))]
-        ranges, lb = [], []
-        for L in leaves:
-            ranges.append([len(lb), len(L)])
-            lb += L
-        nl = len(leaves)
-        if nl == 0:
-            children = np.zeros((0, 2))
-        elif nl == 1:
-            children = [[-1, -1]]
-        else:
-            children = [[-1 - k, k + 1] for k in range(nl - 2)] + [[-1 - (nl - 2), -nl]]
-        return dict(planes=self.planes, node_children=children, leaf_brush_ranges=ranges,
-                    leaf_brushes=lb, brushes=self.brushes, brush_sides=self.sides,
-                    texinfo_flags=self.texinfo, vertexes=self.verts or np.zeros((0, 3)),
-                    edges=self.edges, surf_edges=self.surf or np.zeros(0),
-                    faces=self.faces or np.zeros((0, 3)))
+from vrad_gb300.scenes import BrushMap as World  # noqa: E402  (the lump writer)
 
 
 def _ingest(host_ctx, lumps, **kw):
@@ -285,3 +219,28 @@ def test_many_brushes_keep_the_reference_order(vlib, host_ctx, oracle):
     env, xyz, ids, nb, ns = _ingest(host_ctx, lumps)
     rx, rids, rnb = oracle.bsp_world_triangles(lumps)
     assert nb == rnb > 30000 and np.array_equal(xyz, rx) and np.array_equal(ids, rids)
+
+
+def test_lit_brush_world_faces_follow_the_ingest(host_ctx):
+    # the brush world of the direct-light bench: every triangle its tri_face
+    # maps to a lit face lies in that face's rectangle, the room's brushes and
+    # the sky face map to none, and its walls are ingested brush sides
+    from vrad_gb300 import scenes
+
+    lumps, lit = scenes.lit_brush_world(0, n_faces=600)
+    env, xyz, ids, nb, ns = _ingest(host_ctx, lumps)
+    assert ns == 2 and len(lit.tri_face) == len(ids) == nb + 2 == 12 * (5 + 100) + 2
+    f = lit.tri_face
+    assert (f[:60] == -1).all() and (f[-2:] == -1).all() and (ids[-2:] & SKY).all()
+    m = f >= 0
+    assert np.array_equal(np.unique(f[m]), np.arange(600))
+    v = xyz[m].reshape(-1, 3, 3).astype(np.float64)
+    c, u, w, n = (a[f[m]][:, None, :].astype(np.float64) for a in (lit.corner, lit.u, lit.v, lit.normal))
+    assert np.abs(((v - c) * n).sum(-1)).max() < 1e-3
+    for e in (u, w):
+        s = ((v - c) * e).sum(-1) / (e * e).sum(-1)
+        assert s.min() > -1e-6 and s.max() < 1 + 1e-6
+    env.SetupAccelerationStructure()
+    env.set_faces(lit)
+    tris, counts = env.wall_slots()
+    assert counts.tolist() == [4, 4, 4, 4, 2, 4]  # the outer sides of wall and floor brushes

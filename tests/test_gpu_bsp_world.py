@@ -78,3 +78,30 @@ def test_can_leaf_trace_to_sky_like_the_oracle(gpu_ctx, oracle):
     frac = oracle.Scene(xyz, ids).test_lines(a, b, skip=-1, threads=16)
     want = (frac.reshape(-1, 162) > 0).any(axis=1)
     assert np.array_equal(got, want) and not want[:20].any() and want[20:].mean() > 0.5
+
+
+def test_direct_light_on_a_brush_world_like_the_oracle(gpu_ctx, oracle):
+    # the direct-light gather over boxes and walls ingested as brushes, with
+    # the wall cells on and off: every luxel bit-identical to the oracle's
+    from conftest import bits_equal
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    lumps, lit = scenes.lit_brush_world(3, n_faces=384)
+    ref = None
+    for walls in (True, False):
+        env = Environment(gpu_ctx)
+        env.set_wall_slots(walls)
+        env.add_bsp_world(lumps)
+        env.SetupAccelerationStructure()
+        env.set_faces(lit)
+        env.set_lights(lit.lights)
+        rgb, rays = env.gather_direct_light(supersamples=4, seed=5)
+        if ref is None:
+            xyz, ids = env.get_triangle_vertices()
+            ref, rrays = oracle.gather_luxels(oracle.Scene(xyz, ids), oracle.make_lights(lit.lights),
+                                              len(lit.lights), lit, 0, lit.n_faces, ss=4, seed=5,
+                                              threads=16)
+            assert rays == rrays and np.abs(ref).max() > 0
+        assert bits_equal(rgb, ref)
+        env.close()

@@ -16,6 +16,7 @@ namespace vrg {
 namespace {
 
 constexpr int kThreads = 128;
+static_assert(kThreads <= kShRayLanes, "kOptShRay keeps one slot per thread of a block");
 
 
 // One thread per supersample; the S = 4 samples of a luxel sit in four
@@ -160,10 +161,11 @@ void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst) {
     }
 }
 
-// The seven tuned variants of k_direct_luxels for wall layout WM: samples
+// The eight tuned variants of k_direct_luxels for wall layout WM: samples
 // claimed per warp (32, 64, 128), 32 with the leaf records kept out of L1,
 // 32 in 4 x 2 luxel tiles without and with the top of the tree in shared
-// memory, and in tiles skipping children without triangles.
+// memory, in tiles skipping children without triangles, and in tiles with
+// the walk constants in shared memory.
 template <int WM>
 void launch_direct_variant(int v, int grid, cudaStream_t st, const DevScene &s, const DevLight *lights, int nl,
                            const vrg_env *env, int64_t nlux, int ss, uint64_t seed, float *out_rgb,
@@ -184,8 +186,10 @@ void launch_direct_variant(int v, int grid, cudaStream_t st, const DevScene &s, 
         k_direct_luxels<32, 0, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
     else if (v == 5)
         k_direct_luxels<32, kOptTop, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else
+    else if (v == 6)
         k_direct_luxels<32, kOptSkip, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+    else
+        k_direct_luxels<32, kOptShRay, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
 }
 
 int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
@@ -223,7 +227,7 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 7, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 8, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

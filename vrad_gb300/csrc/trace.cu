@@ -164,6 +164,12 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
                     const LinePlan p = plan_line(s, make_line(sx, sy, sz, ex, ey, ez));
                     ray = p.ray;
                     rp = p.rp;
+                    if (OPT & kOptShRay) {
+#pragma unroll
+                        for (int a = 0; a < 3; a++)
+                            g_ray_axes[a * kShRayLanes + threadIdx.x] = make_float4(
+                                rp.inv[a], rp.A[a], rp.B[a], __uint_as_float((rp.neg >> a) & 1u));
+                    }
                     len = p.len;
                     any_limit = p.any_limit;
                     best = -1;
@@ -341,7 +347,8 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // refill with whole-leaf steps; unit rounds (new lines at 4 or 8 idle
 // lanes, with or without the vote, at the default or a 40-register cap,
 // leaf records kept out of L1 or not, top of the tree in shared memory or
-// not, next plane loaded ahead, children without triangles skipped or not).
+// not, next plane loaded ahead, children without triangles skipped or not,
+// the walk constants in shared memory or not).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
@@ -352,6 +359,7 @@ const MaskKernel kMaskOcc[] = {
     k_trace_unit<false, 4, false, 1, kOptStream | kOptPipe>,
     k_trace_mask<false, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptSkip>,
     k_trace_unit<false, 8, true, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptStream | kOptSkip>,
+    k_trace_unit<false, 4, false, 1, kOptSkip | kOptShRay>, k_trace_unit<false, 8, true, 1, kOptSkip | kOptShRay>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -363,8 +371,10 @@ const MaskKernel kMaskHit[] = {
     k_trace_unit<true, 4, false, 1, kOptStream | kOptPipe>,
     k_trace_mask<true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptSkip>,
     k_trace_unit<true, 8, true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptStream | kOptSkip>,
+    k_trace_unit<true, 4, false, 1, kOptSkip | kOptShRay>, k_trace_unit<true, 8, true, 1, kOptSkip | kOptShRay>,
 };
-constexpr int kMaskVariants = 16;
+constexpr int kMaskVariants = 18;
+static_assert(kThreads <= kShRayLanes, "kOptShRay keeps one slot per thread of a block");
 
 }  // namespace
 

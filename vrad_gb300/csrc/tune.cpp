@@ -45,6 +45,7 @@ int tune_pick(vrg_ctx *ctx, const std::string &key, int nvar,
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
         tune = false;
+    if (nvar > kTuneMaxVariants) return fail(ctx, VRG_ERR_INVALID, "too many variants at a tuned launch site");
     if (!tune || nvar < 2) return VRG_OK;
     cudaEvent_t a = nullptr, b = nullptr;
     VRG_CUDA(ctx, cudaEventCreate(&a));
@@ -134,7 +135,7 @@ int vrg_ctx_autotune_load(vrg_ctx *ctx, const char *path) {
     std::string key;
     int v;
     while (f >> key >> v)
-        if (v >= 0 && v < 16) ctx->tuned[key] = v;
+        if (v >= 0 && v < kTuneMaxVariants) ctx->tuned[key] = v;
     return VRG_OK;
 }
 

@@ -223,6 +223,7 @@ int cuda_fail(vrg_ctx *ctx, cudaError_t e, const char *what);
 // variant, first timing every variant through `launch` when the bucket is
 // new; tune_run then launches the chosen one unless tuning just did.
 std::string tune_key(const char *kernel, int64_t scene_size, int64_t work);
+constexpr int kTuneMaxVariants = 32;  // variants of one launch site, at most
 int tune_pick(vrg_ctx *ctx, const std::string &key, int nvar,
               const std::function<cudaError_t(int)> &launch, int *variant);
 int tune_run(vrg_ctx *ctx, const std::string &key, int nvar,

@@ -37,10 +37,20 @@ constexpr int kOptStream = 1;
 constexpr int kOptTop = 2;
 constexpr int kOptPipe = 8;    // unit rounds: the next triangle's plane loads during this test
 constexpr int kOptSkip = 16;   // children flagged as leaves without triangles are not visited
+// kOptShRay: the walk constants of each lane's ray are kept in shared memory,
+// one float4 (inv, A, B, neg) per axis and lane, and an inner step reads its
+// axis's with one load instead of selecting three of nine registers.  For
+// blocks of at most kShRayLanes threads.
+constexpr int kOptShRay = 32;
+constexpr int kShRayLanes = 128;
 
 // Shared-memory copy of the scene's top table, for kernels walking with
 // kOptTop (allocated only in kernels that use it).
 static __shared__ uint2 g_top_nodes[kTopNodes];
+
+// Per-lane copy of the walk constants for kOptShRay (allocated only in kernels
+// that use it).
+static __shared__ float4 g_ray_axes[3 * kShRayLanes];
 
 // Every thread of the block calls this once, before its first walk.
 __device__ __forceinline__ void stage_top(const DevScene &s) {
@@ -177,10 +187,20 @@ __device__ __forceinline__ bool inner_step(const RayPre &rp, uint2 nd, float &t0
     const uint32_t type = nd.x & 3u;
     const float sv = __uint_as_float(nd.y);
     const uint32_t left = (nd.x >> 2) & kChildIndexMask;
-    const float inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
-    const float A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
-    const float B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
-    const uint32_t neg = (rp.neg >> type) & 1u;
+    float inv, A, B;
+    uint32_t neg;
+    if (OPT & kOptShRay) {
+        const float4 c = g_ray_axes[type * kShRayLanes + threadIdx.x];
+        inv = c.x;
+        A = c.y;
+        B = c.z;
+        neg = __float_as_uint(c.w);
+    } else {
+        inv = pick3((int)type, rp.inv[0], rp.inv[1], rp.inv[2]);
+        A = pick3((int)type, rp.A[0], rp.A[1], rp.A[2]);
+        B = pick3((int)type, rp.B[0], rp.B[1], rp.B[2]);
+        neg = (rp.neg >> type) & 1u;
+    }
     const uint32_t nearc = left + neg, farc = left + 1u - neg;
     const bool near_empty = (OPT & kOptSkip) && (nd.x & (neg ? kRightEmpty : kLeftEmpty)) != 0u;
     const bool far_empty = (OPT & kOptSkip) && (nd.x & (neg ? kLeftEmpty : kRightEmpty)) != 0u;
@@ -339,6 +359,12 @@ template <int MODE, int OPT = 0>
 __device__ int32_t kd_trace(const DevScene &s, const Ray &ray, const RayPre &rp, float slack,
                             float tmin, float tmax, int32_t skip, float any_limit, float *t_out) {
     TraceState st;
+    if (OPT & kOptShRay) {
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            g_ray_axes[a * kShRayLanes + threadIdx.x] =
+                make_float4(rp.inv[a], rp.A[a], rp.B[a], __uint_as_float((rp.neg >> a) & 1u));
+    }
     if (trace_init(s, ray, rp, slack, tmin, tmax, st, root_ref<OPT>(s)))
         while (!trace_step<MODE, 1, OPT>(s, ray, rp, tmin, tmax, skip, any_limit, st)) {
         }

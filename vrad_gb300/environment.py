@@ -99,8 +99,8 @@ class Context:
     def autotune_choice(self, key: str):
         """(variant, per-variant ms) of a tuned bucket; variant -1 if untuned."""
         v = C.c_int32(-1)
-        ms = (C.c_double * 16)()
-        check(self.lib.vrg_ctx_autotune_choice(self.h, key.encode(), C.byref(v), ms, 16),
+        ms = (C.c_double * 32)()  # a launch site has at most 32 variants
+        check(self.lib.vrg_ctx_autotune_choice(self.h, key.encode(), C.byref(v), ms, 32),
               self.h, "autotune_choice")
         return v.value, [x for x in ms if x > 0.0]
 

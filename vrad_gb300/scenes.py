@@ -26,6 +26,9 @@ TRACE_ID_STATICPROP = 0x04000000
 
 EMIT_SURFACE, EMIT_POINT, EMIT_SPOTLIGHT, EMIT_SKYLIGHT, EMIT_QUAKELIGHT, EMIT_SKYAMBIENT = range(6)
 
+# BSP flags a written map uses (texinfo surface flag, brush contents)
+SURF_SKY, CONTENTS_SOLID = 0x4, 0x1
+
 ROOM = 4096.0
 _GAMMA = np.uint64(0x9E3779B97F4A7C15)
 _M1 = np.uint64(0xBF58476D1CE4E5B9)
@@ -274,6 +277,114 @@ def lit_scene(seed: int = 0, n_faces: int = 4096, spacing: float = 16.0, n_point
     return LitScene(xyz, ids, np.asarray(tri_face, np.int32), corner, u, v, nrm, nu, nv,
                     np.full(len(faces), np.float32(1.0 / spacing), np.float32),
                     np.ascontiguousarray(refl, dtype=np.float32), lights)
+
+
+class BrushMap:
+    """Lump arrays of a compiled map, written the way a BSP lays them out
+    (the arrays ``Environment.add_bsp_world`` takes): planes in pairs (p ^ 1
+    faces the other way), brushes over brush sides, leaves over leaf
+    brushes, faces over signed surfedges.  Texinfo 0 is plain, 1 is sky."""
+
+    def __init__(self):
+        self.planes, self.sides, self.brushes = [], [], []
+        self.texinfo = [0, SURF_SKY]  # texinfo 0 plain, 1 sky
+        self.verts, self.edges, self.surf, self.faces = [], [[0, 0]], [], []
+
+    def plane(self, n, d):
+        n = np.asarray(n, np.float32)
+        self.planes += [[*n, d], [*(-n), -d]]
+        return len(self.planes) - 2
+
+    def brush(self, planes, contents=CONTENTS_SOLID, texinfo=None, disp=None, bevel=None):
+        first = len(self.sides)
+        for i, (n, d) in enumerate(planes):
+            self.sides.append([self.plane(n, d), (texinfo or {}).get(i, 0), (disp or {}).get(i, 0),
+                               (bevel or {}).get(i, 0)])
+        self.brushes.append([first, len(planes), contents])
+        return len(self.brushes) - 1
+
+    def box(self, mn, mx, **kw):
+        planes = []
+        for a in range(3):
+            e = np.zeros(3, np.float32)
+            e[a] = 1
+            planes += [(e, float(mx[a])), (-e, -float(mn[a]))]
+        return self.brush(planes, **kw)
+
+    def face(self, pts, texinfo=1, flip_every=2):
+        first = len(self.surf)
+        base = len(self.verts)
+        self.verts += [list(p) for p in pts]
+        n = len(pts)
+        for j in range(n):
+            a, b = base + j, base + (j + 1) % n
+            if j % flip_every == 1:  # stored the other way round: read through -edge
+                self.edges.append([b, a])
+                self.surf.append(-(len(self.edges) - 1))
+            else:
+                self.edges.append([a, b])
+                self.surf.append(len(self.edges) - 1)
+        self.faces.append([first, n, texinfo])
+
+    def lumps(self, leaves=None):
+        """leaves: brush lists of the leaves, which a chain of nodes visits in
+        order (node k: leaf k in front, node k + 1 behind; the last node has
+        the last two leaves; one leaf sits on both sides of node 0)."""
+        leaves = leaves if leaves is not None else [list(range(len(self.brushes)))]
+        ranges, lb = [], []
+        for L in leaves:
+            ranges.append([len(lb), len(L)])
+            lb += L
+        nl = len(leaves)
+        if nl == 0:
+            children = np.zeros((0, 2))
+        elif nl == 1:
+            children = [[-1, -1]]
+        else:
+            children = [[-1 - k, k + 1] for k in range(nl - 2)] + [[-1 - (nl - 2), -nl]]
+        return dict(planes=self.planes, node_children=children, leaf_brush_ranges=ranges,
+                    leaf_brushes=lb, brushes=self.brushes, brush_sides=self.sides,
+                    texinfo_flags=self.texinfo, vertexes=self.verts or np.zeros((0, 3)),
+                    edges=self.edges, surf_edges=self.surf or np.zeros(0),
+                    faces=self.faces or np.zeros((0, 3)))
+
+
+def lit_brush_world(seed: int = 0, n_faces: int = 4096, spacing: float = 16.0,
+                    thick: float = 16.0):
+    """The scene of ``lit_scene(seed, n_faces, spacing)`` -- its lit box faces
+    and its lights -- with the room and the boxes written as brushes of a
+    compiled map: a floor and four walls ``thick`` units thick around the
+    same 4096-unit room, a sky face closing its top, and one box brush per
+    box.  Returns (lumps, lit): the triangles are what ``add_bsp_world``
+    makes of the lumps (``lit.xyz`` / ``lit.ids`` are empty), and
+    ``lit.tri_face`` follows their order -- the room's five brushes, then
+    each box's six sides in plane order (+x, -x, +y, -y, +z, -z, two
+    triangles each), then the sky face."""
+    lit = lit_scene(seed, n_faces=n_faces, spacing=spacing)
+    n_boxes = (n_faces + 5) // 6
+    mins, maxs = _random_boxes(Stream(seed, S_BOXES), n_boxes, 64.0, 512.0)
+    w = BrushMap()
+    t, L = float(thick), ROOM
+    w.box((-t, -t, -t), (L + t, L + t, 0.0))  # floor
+    w.box((-t, -t, 0.0), (0.0, L + t, L))
+    w.box((L, -t, 0.0), (L + t, L + t, L))
+    w.box((0.0, -t, 0.0), (L, 0.0, L))
+    w.box((0.0, L, 0.0), (L, L + t, L))
+    w.face([(0.0, 0.0, L), (L, 0.0, L), (L, L, L), (0.0, L, L)], texinfo=1)
+    for b in range(n_boxes):
+        w.box(tuple(float(c) for c in mins[b]), tuple(float(c) for c in maxs[b]))
+    # box_quads' face order is z max, z min, x min, x max, y max, y min
+    side_face = (3, 2, 4, 5, 0, 1)
+    tri_face = [-1] * (5 * 12)
+    for b in range(n_boxes):
+        for s in range(6):
+            f = 6 * b + side_face[s]
+            tri_face += [f, f] if f < n_faces else [-1, -1]
+    tri_face += [-1, -1]  # the sky face's two triangles
+    lit.xyz = np.zeros((0, 9), np.float32)
+    lit.ids = np.zeros(0, np.int32)
+    lit.tri_face = np.asarray(tri_face, np.int32)
+    return w.lumps(), lit
 
 
 def transfer_directions(k: int) -> np.ndarray:
