@@ -301,7 +301,9 @@ def _trace_roofline(kernel, units, avg_ms, bytes_per_unit, hbm_peak, hbm_kind, l
     count is the tuned variant's own (`warp_instructions_per_unit_v<n>`)
     where the summary has it."""
     alg = bytes_per_unit * units / (avg_ms * 1e-3) / 1e9
-    traffic = _ncu_traffic(prof)
+    traffic = _profile_value(prof, f"dram_bytes_per_launch_full_v{variant}") if variant is not None else None
+    if traffic is None:
+        traffic = _ncu_traffic(prof)
     sm_mhz = (clk or {}).get("sm_mhz")
     inst = _profile_value(prof, f"warp_instructions_per_unit_v{variant}") if variant is not None else None
     inst_of = f"variant {variant}" if inst is not None else "the variant the summary names"
@@ -424,7 +426,10 @@ def run_gpu(args, rank, world, local_rank):
         t0 = time.perf_counter()
         step_host()
         e2e_t.append(time.perf_counter() - t0)
-    e2e_value = units * world / statistics.mean(e2e_t) / 1e6
+    # the median step: one host stall in a few wall-clock steps would move the
+    # mean by itself (the mean is reported beside it)
+    e2e_value = units * world / statistics.median(e2e_t) / 1e6
+    e2e_mean = units * world / statistics.mean(e2e_t) / 1e6
 
     if rank != 0:
         if dist:
@@ -484,7 +489,8 @@ def run_gpu(args, rank, world, local_rank):
                    "setup_acceleration_structure_ms": admit_ms},
         "parity": parity,
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "statistic": f"median of {len(e2e_t)} wall-clock steps",
+                "mean_value": round(e2e_mean, 3)},
         "gpu_launches": int(launches),
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -577,13 +583,13 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
     tv, tms = lib_ctx.autotune_choice(Context.tune_key("trace_mask", env.num_triangles(), n))
     hv, hms = lib_ctx.autotune_choice(Context.tune_key("trace_mask_hit", env.num_triangles(), n))
     # the device's walk, counted by the oracle on the device's tree
-    skip_empty = tv in (12, 13, 14, 15, 16, 17)
+    skip_empty = tv in (12, 13, 14, 15, 16, 17, 18)
     s.set_tree(*env.walk_tree()[:3])
     s.set_skip_empty(skip_empty)
     _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
     nodes, tris = st[:, 0].mean(), st[:, 1].mean()
     bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
-    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15, 16, 17) else (
+    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15, 16, 17, 18) else (
         "ncu_trace_unit_stream.txt" if tv in (6, 7, 9, 10, 11) else "ncu_trace_mask.txt")
     peak, kind = _peaks()
     avg_ms = kms / max(kn, 1)
@@ -600,8 +606,10 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
         "closest_hit": {"value": round(n / (statistics.mean(hit_ms) * 1e-3) / 1e6, 3),
                         "unit": "Mrays/s", "ms_per_step": round(statistics.mean(hit_ms), 4),
                         "outputs": "mask + hit index + t", "autotune_variant": hv},
-        "e2e": {"value": round(n / statistics.mean(e2e) / 1e6, 3), "unit": "Mrays/s",
-                "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 4 * ((n + 31) // 32)},
+        "e2e": {"value": round(n / statistics.median(e2e) / 1e6, 3), "unit": "Mrays/s",
+                "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 4 * ((n + 31) // 32),
+                "statistic": f"median of {len(e2e)} wall-clock steps",
+                "mean_value": round(n / statistics.mean(e2e) / 1e6, 3)},
         "parity": {"oracle": "C restatement, all 2^20 lines", "mask_bits_differing": diff_bits,
                    "hit_index_differing": int(np.count_nonzero(got_h != rh)),
                    "t_bits_differing": int(np.count_nonzero(got_t.view(np.uint32) != rt.view(np.uint32))),

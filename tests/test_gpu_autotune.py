@@ -47,7 +47,7 @@ def test_trace_mask_variants_identical(gpu_ctx, anyhit_scene, tmp_path):
     for closest in (False, True):
         key = Context.tune_key("trace_mask_hit" if closest else "trace_mask", env.num_triangles(), n)
         outs = []
-        for v in range(18):
+        for v in range(19):
             _force(gpu_ctx, tmp_path, key, v)
             outs.append(env.occlusion_mask(a, b, closest=closest))
         for o in outs[1:]:
@@ -72,8 +72,8 @@ def test_direct_variants_identical_and_choice_recorded(gpu_ctx, tmp_path):
     assert gpu_ctx.autotune_choice(key)[0] == -1
     rgb0, rays0 = env.gather_direct_light(supersamples=4, seed=2)  # tunes this bucket
     v, ms = gpu_ctx.autotune_choice(key)
-    assert v in range(8) and len(ms) == 8
-    for v in range(8):
+    assert v in range(12) and len(ms) == 12
+    for v in range(12):
         _force(gpu_ctx, tmp_path, key, v)
         rgb, rays = env.gather_direct_light(supersamples=4, seed=2)
         assert rays == rays0

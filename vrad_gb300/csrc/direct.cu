@@ -30,8 +30,8 @@ static_assert(kThreads <= kShRayLanes, "kOptShRay keeps one slot per thread of a
 // TILE walks each face's luxels in 4 x 2 tiles (tile_luxel) instead of row
 // order; the output is the same, each luxel written by the lane holding its
 // first sample.  WM is the scene's wall layout (slots or cells).
-template <int FETCH, int OPT = 0, bool TILE = false, int WM = kWallSlotsOnly>
-__global__ void __launch_bounds__(kThreads, 8) k_direct_luxels(
+template <int FETCH, int OPT = 0, bool TILE = false, int WM = kWallSlotsOnly, int MINB = 8>
+__global__ void __launch_bounds__(kThreads, MINB) k_direct_luxels(
     DevScene s, const DevLight *__restrict__ lights, int nl, const FaceRec *__restrict__ faces,
     const int64_t *__restrict__ off, int nfaces, int64_t nlux, int ss, uint64_t seed,
     float *__restrict__ out, const float *__restrict__ pts, const float *__restrict__ nrm, int64_t npts,
@@ -161,35 +161,51 @@ void pack_lights(const std::vector<vrg_light> &src, std::vector<float4> &dst) {
     }
 }
 
-// The eight tuned variants of k_direct_luxels for wall layout WM: samples
+// A persistent launch of kernel k: one wave of the blocks k keeps resident
+// per SM, or fewer when the work is small.
+template <class K>
+void launch_direct(K k, int64_t need, int sms, cudaStream_t st, const DevScene &s, const DevLight *lights, int nl,
+                   const vrg_env *env, int64_t nlux, int ss, uint64_t seed, float *out_rgb, const float *pts,
+                   const float *nrm, int64_t npts, float *pts_out, unsigned long long *d_rays,
+                   unsigned long long *work) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 4;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sms * per_sm));
+    k<<<grid, kThreads, 0, st>>>(s, lights, nl, env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(),
+                                 env->nfaces, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+}
+
+// The twelve tuned variants of k_direct_luxels for wall layout WM: samples
 // claimed per warp (32, 64, 128), 32 with the leaf records kept out of L1,
 // 32 in 4 x 2 luxel tiles without and with the top of the tree in shared
-// memory, in tiles skipping children without triangles, and in tiles with
-// the walk constants in shared memory.
+// memory, in tiles skipping children without triangles, in tiles with the
+// walk constants in shared memory at 8, 9 or 10 resident blocks per SM (64,
+// 56 or 48 registers), in plain tiles at 9 blocks, and in tiles with the
+// walk constants and the top of the tree in shared memory at 9 blocks.
 template <int WM>
-void launch_direct_variant(int v, int grid, cudaStream_t st, const DevScene &s, const DevLight *lights, int nl,
-                           const vrg_env *env, int64_t nlux, int ss, uint64_t seed, float *out_rgb,
-                           const float *pts, const float *nrm, int64_t npts, float *pts_out,
-                           unsigned long long *d_rays, unsigned long long *work) {
-    const FaceRec *faces = env->d_faces.as<FaceRec>();
-    const int64_t *off = env->d_luxel_offset.as<int64_t>();
-    const int nf = env->nfaces;
-    if (v == 0)
-        k_direct_luxels<32, 0, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else if (v == 1)
-        k_direct_luxels<64, 0, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else if (v == 2)
-        k_direct_luxels<128, 0, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else if (v == 3)
-        k_direct_luxels<32, kOptStream, false, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else if (v == 4)
-        k_direct_luxels<32, 0, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else if (v == 5)
-        k_direct_luxels<32, kOptTop, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else if (v == 6)
-        k_direct_luxels<32, kOptSkip, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
-    else
-        k_direct_luxels<32, kOptShRay, true, WM><<<grid, kThreads, 0, st>>>(s, lights, nl, faces, off, nf, nlux, ss, seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
+void launch_direct_variant(int v, int64_t need, int sms, cudaStream_t st, const DevScene &s,
+                           const DevLight *lights, int nl, const vrg_env *env, int64_t nlux, int ss,
+                           uint64_t seed, float *out_rgb, const float *pts, const float *nrm, int64_t npts,
+                           float *pts_out, unsigned long long *d_rays, unsigned long long *work) {
+#define VRG_DIRECT(...) \
+    launch_direct(k_direct_luxels<__VA_ARGS__>, need, sms, st, s, lights, nl, env, nlux, ss, seed, out_rgb, pts, \
+                  nrm, npts, pts_out, d_rays, work)
+    switch (v) {
+    case 0: VRG_DIRECT(32, 0, false, WM); break;
+    case 1: VRG_DIRECT(64, 0, false, WM); break;
+    case 2: VRG_DIRECT(128, 0, false, WM); break;
+    case 3: VRG_DIRECT(32, kOptStream, false, WM); break;
+    case 4: VRG_DIRECT(32, 0, true, WM); break;
+    case 5: VRG_DIRECT(32, kOptTop, true, WM); break;
+    case 6: VRG_DIRECT(32, kOptSkip, true, WM); break;
+    case 7: VRG_DIRECT(32, kOptShRay, true, WM); break;
+    case 8: VRG_DIRECT(32, kOptShRay, true, WM, 9); break;
+    case 9: VRG_DIRECT(32, kOptShRay, true, WM, 10); break;
+    case 10: VRG_DIRECT(32, 0, true, WM, 9); break;
+    default: VRG_DIRECT(32, kOptShRay | kOptTop, true, WM, 9); break;
+    }
+#undef VRG_DIRECT
 }
 
 int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
@@ -200,12 +216,7 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
     if (nlux == 0 && npts == 0) return VRG_OK;
     VRG_CUDA(ctx, env->d_work.reserve(256));
     unsigned long long *work = env->d_work.as<unsigned long long>() + 1;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_luxels<32>, kThreads, 0) != cudaSuccess ||
-        per_sm < 1)
-        per_sm = 4;
     const int64_t need = (nlux * ss + npts + kThreads - 1) / kThreads;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->num_sms * per_sm));
     const DevScene s = scene_view(env);
     const DevLight *lights = env->d_lights.as<DevLight>();
     const int nl = (int)env->lights.size();
@@ -218,16 +229,16 @@ int launch_gather_luxels(vrg_env *env, int ss, uint64_t seed, float *out_rgb,
         cudaEvent_t ev = nullptr;
         timing_begin(ctx, "direct_luxels", &ev);
         if (env->wall_layout == 0)
-            launch_direct_variant<kWallSlotsOnly>(v, grid, ctx->stream, s, lights, nl, env, nlux, ss, seed, out_rgb,
-                                                  pts, nrm, npts, pts_out, d_rays, work);
+            launch_direct_variant<kWallSlotsOnly>(v, need, ctx->num_sms, ctx->stream, s, lights, nl, env, nlux, ss,
+                                                  seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         else
-            launch_direct_variant<kWallCellsOnly>(v, grid, ctx->stream, s, lights, nl, env, nlux, ss, seed, out_rgb,
-                                                  pts, nrm, npts, pts_out, d_rays, work);
+            launch_direct_variant<kWallCellsOnly>(v, need, ctx->num_sms, ctx->stream, s, lights, nl, env, nlux, ss,
+                                                  seed, out_rgb, pts, nrm, npts, pts_out, d_rays, work);
         e = cudaGetLastError();
         timing_end(ctx, "direct_luxels", ev);
         return e;
     };
-    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 8, launch);
+    return tune_run(ctx, tune_key("direct_luxels", env->geom.ntris, nlux * ss + npts), 12, launch);
 }
 
 int launch_gather_points(vrg_env *env, const float *pts, const float *nrm, int64_t n,

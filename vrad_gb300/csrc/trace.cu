@@ -360,6 +360,7 @@ const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptSkip>,
     k_trace_unit<false, 8, true, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptStream | kOptSkip>,
     k_trace_unit<false, 4, false, 1, kOptSkip | kOptShRay>, k_trace_unit<false, 8, true, 1, kOptSkip | kOptShRay>,
+    k_trace_unit<false, 8, true, 12, kOptSkip | kOptShRay>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -372,8 +373,9 @@ const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptSkip>,
     k_trace_unit<true, 8, true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptStream | kOptSkip>,
     k_trace_unit<true, 4, false, 1, kOptSkip | kOptShRay>, k_trace_unit<true, 8, true, 1, kOptSkip | kOptShRay>,
+    k_trace_unit<true, 8, true, 12, kOptSkip | kOptShRay>,
 };
-constexpr int kMaskVariants = 18;
+constexpr int kMaskVariants = 19;
 static_assert(kThreads <= kShRayLanes, "kOptShRay keeps one slot per thread of a block");
 
 }  // namespace
