@@ -834,7 +834,7 @@ def sub_batch(args, lib_ctx, stream, dev, flush, l2, sms):
     import torch
 
     from vrad_gb300 import scenes
-    from vrad_gb300.environment import Batch, Environment
+    from vrad_gb300.environment import Batch, Context, Environment
 
     ctx = lib_ctx
     t0 = time.perf_counter()
@@ -883,6 +883,9 @@ def sub_batch(args, lib_ctx, stream, dev, flush, l2, sms):
                   if a["patch_total"].size else 0.0
                   for a, b in zip(outs["plain"], outs["batched"]))
     n = len(envs)
+    gkey = Context.tune_key("batch_gather", sum(env.num_triangles() for env in envs),
+                            sum(env.num_luxels() * 4 + nl for env, nl in zip(envs, leaves)))
+    gv, gms = ctx.autotune_choice(gkey)
     for env in envs:
         env.close()
     batch.close()
@@ -898,7 +901,8 @@ def sub_batch(args, lib_ctx, stream, dev, flush, l2, sms):
                    "transfer_rays_per_patch": args.batch_k,
                    "nnz_per_row": round(sum(nnzs) / max(sum(leaves), 1), 1),
                    "luxels": sum(l.n_luxels for l in lits), "faces": sum(l.n_faces for l in lits),
-                   "leaf_patches": sum(leaves), "setup_s": round(setup_s, 1)},
+                   "leaf_patches": sum(leaves), "setup_s": round(setup_s, 1),
+                   "autotune": {"bucket": gkey, "variant": gv, "variant_ms": [round(x, 3) for x in gms]}},
         "plain": {"bakes_per_s": round(n / res["plain"][0], 2), "ms_per_batch": round(1e3 * res["plain"][0], 2)},
         "batched": {"bakes_per_s": round(n / res["batched"][0], 2),
                     "ms_per_batch": round(1e3 * res["batched"][0], 2)},

@@ -128,7 +128,7 @@ int64_t vrg_ctx_launch_count(const vrg_ctx *ctx);
 
 /* Per-scene-size autotuning (no reference counterpart).  Tuned launch
  * sites ("trace_mask", "trace_mask_hit", "direct_luxels", "transfer_rows",
- * "bounce_spmv") offer variants that give identical results (the bounce
+ * "bounce_spmv", "batch_gather") offer variants that give identical results (the bounce
  * variants: the same sums); the first launch in a bucket
  * "<site>/t<log2 triangles>/n<log2 work items>" times each twice on the real
  * input and keeps the fastest.  On by default; off, or inside a stream

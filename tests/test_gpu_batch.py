@@ -88,3 +88,33 @@ def test_batch_rejects_unprepared_scene(gpu_ctx):
     batch.add(env)
     with pytest.raises(VrgError, match="call out of order"):
         batch.bake()
+
+
+def test_batch_gather_variants_identical(small_batch, gpu_ctx, tmp_path):
+    # the register walk and the walk with its constants in shared memory give
+    # the same luxels, leaf-point light and shadow-ray count
+    from vrad_gb300.environment import Batch, Context
+
+    lits, envs = small_batch
+    tris = sum(env.num_triangles() for env, _ in envs)
+    items = sum(env.num_luxels() * 4 + nl for env, nl in envs)
+    key = Context.tune_key("batch_gather", tris, items)
+    outs = []
+    for v in range(3):
+        p = tmp_path / f"tune_batch_{v}.txt"
+        p.write_text(f"{key} {v}\n")
+        gpu_ctx.autotune_load(str(p))
+        assert gpu_ctx.autotune_choice(key)[0] == v
+        batch = Batch(gpu_ctx)
+        for env, _ in envs:
+            batch.add(env)
+        rays = batch.bake(4, 11, 3, 0.0)
+        outs.append((rays, [env.get_bake(nl) for env, nl in envs]))
+    r0, b0 = outs[0]
+    assert r0 > 0
+    for r1, b1 in outs[1:]:
+        assert r1 == r0
+        for x, y in zip(b0, b1):
+            assert np.array_equal(x["luxels"], y["luxels"])
+            assert np.array_equal(x["patch_direct"], y["patch_direct"])
+            assert np.array_equal(x["patch_total"], y["patch_total"])

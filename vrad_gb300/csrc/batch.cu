@@ -24,6 +24,7 @@ namespace vrg {
 namespace {
 
 constexpr int kThreads = 128;
+static_assert(kThreads <= kShRayLanes, "kOptShRay keeps one slot per thread of a block");
 constexpr int kSpmvThreads = 256;
 constexpr int kGraphBounces = 8;
 
@@ -64,7 +65,9 @@ __device__ __forceinline__ int upper_segment(const int64_t *__restrict__ start, 
 
 // Work items: segments [0, E) are scene e's luxel supersamples (ss per
 // luxel, in luxel order), segments [E, 2E) scene e's leaf-patch points.
-__global__ void __launch_bounds__(kThreads, 8) k_batch_gather(
+// OPT: walk options (kOptShRay or none); MINB: resident blocks per SM.
+template <int OPT, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_batch_gather(
     const BatchDesc *__restrict__ descs, const int64_t *__restrict__ seg, int nscenes, int ss,
     uint64_t seed, unsigned long long *__restrict__ work, unsigned long long *__restrict__ ray_count) {
     const int64_t total = __ldg(seg + 2 * nscenes);
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_batch_gather(
                 ny = __ldg(n + 1);
                 nz = __ldg(n + 2);
             }
-            gather_point<kSkyTrace>(d->scene, d->lights, d->nl, px, py, pz, nx, ny, nz, r, g, b, rays);
+            gather_point<kSkyTrace, OPT>(d->scene, d->lights, d->nl, px, py, pz, nx, ny, nz, r, g, b, rays);
             if (!luxel_item) {
                 float *o = d->pout + 3 * local;
                 o[0] = r;
@@ -371,18 +374,36 @@ int vrg_batch_bake(vrg_batch *b, int32_t supersamples, uint64_t seed, int32_t ma
     SceneCtl *ctl = b->d_ctl.as<SceneCtl>();
     float2 *rowabs = b->d_rowabs.as<float2>();
 
-    // direct pass: one persistent launch over every scene
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_gather, kThreads, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 4;
+    // direct pass: one persistent launch over every scene, in the variant
+    // tuned for the batch's size (the register walk at 8 blocks per SM, or
+    // the walk constants in shared memory at 9 or 8; the same results)
+    using GatherKernel = void (*)(const BatchDesc *, const int64_t *, int, int, uint64_t, unsigned long long *,
+                                  unsigned long long *);
+    const GatherKernel gvar[3] = {k_batch_gather<0, 8>, k_batch_gather<kOptShRay, 9>,
+                                  k_batch_gather<kOptShRay, 8>};
     const int64_t items = seg[2 * E];
-    const int ggrid = (int)std::max<int64_t>(1, std::min<int64_t>((items + kThreads - 1) / kThreads,
-                                                                  (int64_t)ctx->num_sms * per_sm));
+    int64_t tris = 0;
+    for (vrg_env *env : b->envs) tris += env->geom.ntris;
     cudaEvent_t ev = nullptr;
-    timing_begin(ctx, "batch_gather", &ev);
-    k_batch_gather<<<ggrid, kThreads, 0, st>>>(dd, dseg, E, supersamples, seed, cnt, out_shadow_rays ? cnt + 1 : nullptr);
-    VRG_CUDA(ctx, cudaGetLastError());
-    timing_end(ctx, "batch_gather", ev);
+    auto gather = [&](int v) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(cnt, 0, 16, st);  // work queue and shadow rays
+        if (e != cudaSuccess) return e;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gvar[v], kThreads, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 4;
+        const int ggrid = (int)std::max<int64_t>(1, std::min<int64_t>((items + kThreads - 1) / kThreads,
+                                                                      (int64_t)ctx->num_sms * per_sm));
+        timing_begin(ctx, "batch_gather", &ev);
+        gvar[v]<<<ggrid, kThreads, 0, st>>>(dd, dseg, E, supersamples, seed, cnt, out_shadow_rays ? cnt + 1 : nullptr);
+        e = cudaGetLastError();
+        timing_end(ctx, "batch_gather", ev);
+        return e;
+    };
+    {
+        const int rc = tune_run(ctx, tune_key("batch_gather", tris, items), 3, gather);
+        if (rc != VRG_OK) return rc;
+    }
 
     // bounce: block-diagonal over every scene, per-scene stop
     const int ib = (int)std::min<int64_t>(std::max<int64_t>((rows + 255) / 256, 1), (int64_t)ctx->num_sms * 8);
