@@ -781,6 +781,41 @@ int vrg_env_make_patches(vrg_env *env, float max_chop, float min_chop, int64_t *
         info[l].refl = make_float4(env->f_refl[3 * f], env->f_refl[3 * f + 1], env->f_refl[3 * f + 2], fbits);
         info[l].base = make_float4(env->f_base[3 * f], env->f_base[3 * f + 1], env->f_base[3 * f + 2], 0.0f);
     }
+    // per face, for the lightmap kernel's shared-memory copy of the face's
+    // tree: (first node below the root, nodes below the root, first leaf,
+    // leaves).  The subdivision appends a face's nodes in one run and numbers
+    // leaves in node order, so both ranges are contiguous; a face where the
+    // check below fails gets (-1, 0, -1, 0) and is walked in global memory.
+    std::vector<int4> face_tree(std::max<int32_t>(env->nfaces, 1), make_int4(-1, 0, -1, 0));
+    {
+        const int32_t nf = env->nfaces;
+        std::vector<int64_t> n0(nf, INT64_MAX), n1(nf, -1), nc(nf, 0), l0(nf, INT64_MAX), l1(nf, -1), lc(nf, 0);
+        std::vector<char> mixed(nf, 0);  // a child of another face: walk in global memory
+        for (size_t i = 0; i < n; i++) {
+            const int32_t f = P.face[i];
+            if (f < 0 || f >= nf) continue;
+            for (const int32_t c : {P.child1[i], P.child2[i]})
+                if (c >= 0 && ((size_t)c >= n || P.face[c] != f)) mixed[f] = 1;
+            if (P.parent[i] >= 0) {
+                n0[f] = std::min<int64_t>(n0[f], (int64_t)i);
+                n1[f] = std::max<int64_t>(n1[f], (int64_t)i);
+                nc[f]++;
+            }
+            if (P.child1[i] < 0) {
+                l0[f] = std::min<int64_t>(l0[f], P.leaf_index[i]);
+                l1[f] = std::max<int64_t>(l1[f], P.leaf_index[i]);
+                lc[f]++;
+            }
+        }
+        for (int32_t f = 0; f < nf; f++) {
+            if (P.face_root[f] < 0 || lc[f] == 0 || mixed[f]) continue;
+            const bool nodes_run = nc[f] == 0 || n1[f] - n0[f] + 1 == nc[f];
+            const bool leaves_run = l1[f] - l0[f] + 1 == lc[f];
+            if (nodes_run && leaves_run && nc[f] < INT32_MAX && lc[f] < INT32_MAX)
+                face_tree[f] = make_int4(nc[f] ? (int32_t)n0[f] : 0, (int32_t)nc[f], (int32_t)l0[f], (int32_t)lc[f]);
+        }
+    }
+    TRY(upload(ctx, env->d_face_tree, face_tree.data(), face_tree.size() * sizeof(int4)));
     TRY(upload(ctx, env->d_patch_nodes, nodes.data(), nodes.size() * sizeof(PatchNode)));
     TRY(upload(ctx, env->d_leaf_info, info.data(), info.size() * sizeof(LeafInfo)));
     TRY(upload(ctx, env->d_face_root, P.face_root.data(), std::max<size_t>(1, P.face_root.size()) * 4));

@@ -61,19 +61,32 @@ __device__ __forceinline__ uint32_t encode_sample(float r, float g, float b) {
            ((uint32_t)(uint8_t)(int8_t)x << 24);
 }
 
+// A face's patch tree and its leaves' bounced light in shared memory: the
+// root and up to kLmNodes - 1 nodes below it, up to kLmLeaves leaves.
+constexpr int kLmNodes = 256;
+constexpr int kLmLeaves = 128;
+
 // One block per face, faces taken in order from a work counter (zeroed
 // before the launch), so that the blocks that draw large faces do not set
-// the tail as a static stride over faces did: every thread reads the same
-// face record (one broadcast), the threads take the face's luxels in order
-// (coalesced 12-byte reads and 4-byte writes), and the face's patch-tree
-// nodes stay in L1 while its luxels descend them.  No luxel -> face search.
+// the tail as a static stride over faces did.  Every thread reads the same
+// face record (one broadcast); the block copies the face's patch tree and
+// its leaves' totals (face_tree: first node below the root, their count,
+// first leaf, leaf count) into shared memory with coalesced loads, so that
+// each luxel's descent is a chain of shared loads instead of dependent
+// global ones; the threads then take the face's luxels in order (coalesced
+// 12-byte reads and 4-byte writes).  A face whose tree does not fit, or
+// whose ranges the host could not vouch for, is walked in global memory.
+// No luxel -> face search.
 __global__ void __launch_bounds__(kThreads) k_lightmap(
     const FaceRec *__restrict__ faces, const int64_t *__restrict__ off, int nfaces,
     const float *__restrict__ rgb, const float4 *__restrict__ total, const PatchNode *__restrict__ pnodes,
-    const int32_t *__restrict__ face_root, uint32_t *__restrict__ out, unsigned int *__restrict__ work) {
+    const int32_t *__restrict__ face_root, const int4 *__restrict__ face_tree, uint32_t *__restrict__ out,
+    unsigned int *__restrict__ work) {
     __shared__ int face_sh;
+    __shared__ PatchNode sn[kLmNodes];
+    __shared__ float4 sl[kLmLeaves];
     for (;;) {
-        __syncthreads();  // every thread has read the previous face number
+        __syncthreads();  // every thread is done with the previous face
         if (threadIdx.x == 0) face_sh = (int)atomicAdd(work, 1u);
         __syncthreads();
         const int f = face_sh;
@@ -82,17 +95,47 @@ __global__ void __launch_bounds__(kThreads) k_lightmap(
         const int64_t base = __ldg(off + f);
         const int64_t n = __ldg(off + f + 1) - base;
         const int32_t root = __ldg(face_root + f);
+        const int4 ft = __ldg(face_tree + f);
+        const bool staged = root >= 0 && ft.x >= 0 && ft.y < kLmNodes && ft.z >= 0 && ft.w >= 1 &&
+                            ft.w <= kLmLeaves;
+        if (staged) {  // block-uniform
+            for (int i = threadIdx.x; i <= ft.y; i += blockDim.x) sn[i] = pnodes[i == 0 ? root : ft.x + i - 1];
+            for (int i = threadIdx.x; i < ft.w; i += blockDim.x) sl[i] = total[ft.z + i];
+        }
+        __syncthreads();
+        // the luxel centres as luxel_sample places them (one sample, no
+        // jitter), with the face's reciprocals taken once
+        const float inu = rrcp((float)fr.nu), inv = rrcp((float)fr.nv);
         for (int64_t local = threadIdx.x; local < n; local += blockDim.x) {
             const int64_t lux = base + local;
-            const int iv = (int)(local / fr.nu);
-            const int iu = (int)(local - (int64_t)iv * fr.nu);
+            int iv, iu;
+            if (n <= INT32_MAX) {  // block-uniform: 32-bit division
+                iv = (int)local / fr.nu;
+                iu = (int)local - iv * fr.nu;
+            } else {
+                iv = (int)(local / fr.nu);
+                iu = (int)(local - (int64_t)iv * fr.nu);
+            }
             float r = __ldg(rgb + 3 * lux), g = __ldg(rgb + 3 * lux + 1), b = __ldg(rgb + 3 * lux + 2);
             if (root >= 0) {
-                float px, py, pz;
-                luxel_sample(fr, lux, iu, iv, 0, 1, 0, px, py, pz);
-                PatchNode pn = pnodes[root];
-                while (pn.axis >= 0) pn = pnodes[pick3(pn.axis, px, py, pz) >= pn.dist ? pn.child1 : pn.child2];
-                const float4 t = total[pn.leaf];
+                const float su = rmul(radd((float)iu, 0.5f), inu), sv = rmul(radd((float)iv, 0.5f), inv);
+                const float px = radd(radd(radd(fr.corner.x, rmul(fr.u.x, su)), rmul(fr.v.x, sv)),
+                                      rmul(fr.normal.x, kSampleOffset));
+                const float py = radd(radd(radd(fr.corner.y, rmul(fr.u.y, su)), rmul(fr.v.y, sv)),
+                                      rmul(fr.normal.y, kSampleOffset));
+                const float pz = radd(radd(radd(fr.corner.z, rmul(fr.u.z, su)), rmul(fr.v.z, sv)),
+                                      rmul(fr.normal.z, kSampleOffset));
+                float4 t;
+                if (staged) {
+                    PatchNode pn = sn[0];
+                    while (pn.axis >= 0)
+                        pn = sn[1 + (pick3(pn.axis, px, py, pz) >= pn.dist ? pn.child1 : pn.child2) - ft.x];
+                    t = sl[pn.leaf - ft.z];
+                } else {
+                    PatchNode pn = pnodes[root];
+                    while (pn.axis >= 0) pn = pnodes[pick3(pn.axis, px, py, pz) >= pn.dist ? pn.child1 : pn.child2];
+                    t = total[pn.leaf];
+                }
                 r = radd(r, t.x);
                 g = radd(g, t.y);
                 b = radd(b, t.z);
@@ -133,7 +176,8 @@ int vrg_env_get_lightmap(vrg_env *env, uint8_t *samples, int64_t *face_offset) {
     k_lightmap<<<grid, kThreads, 0, st>>>(env->d_faces.as<FaceRec>(), env->d_luxel_offset.as<int64_t>(),
                                          env->nfaces, env->d_bake_rgb.as<float>(),
                                          env->d_total.as<float4>(), env->d_patch_nodes.as<PatchNode>(),
-                                         env->d_face_root.as<int32_t>(), env->d_out0.as<uint32_t>(), work);
+                                         env->d_face_root.as<int32_t>(), env->d_face_tree.as<int4>(),
+                                         env->d_out0.as<uint32_t>(), work);
     VRG_CUDA(ctx, cudaGetLastError());
     timing_end(ctx, "lightmap", ev);
     VRG_CUDA(ctx, cudaMemcpyAsync(samples, env->d_out0.ptr, 4 * (size_t)nlux, cudaMemcpyDeviceToHost, st));

@@ -172,6 +172,7 @@ struct vrg_env {
     bool have_patches = false;
     PatchSet patches;
     vrg::DevBuf d_patch_nodes, d_leaf_info, d_face_root;
+    vrg::DevBuf d_face_tree;  // int4 per face: see face_tree_ranges (capi.cpp)
     bool have_transfers = false;
     int64_t nnz = 0;
     int32_t transfer_k = 0;
