@@ -790,6 +790,30 @@ def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
     bytes_iter = 8 * nnz + 72 * nl  # col+weight per entry; row_ptr, refl, total RMW, emit out per row
     achieved = bytes_iter / (per_iter_ms * 1e-3) / 1e9
     traffic_k = _profile_value("ncu_bounce_spmv.txt", "dram_bytes_per_entry")
+    # the lightmap samples of a whole bake of this scene (direct + bounce):
+    # the kernel timed per launch with L2 flushed before each call, every
+    # sample compared with the oracle's encoding of the same bake
+    import torch
+
+    env.bake(4, SEED, 100, 1e-3)
+    res = env.get_bake(nl)
+    env.get_lightmap()
+    ctx.set_timing(True)
+    ctx.reset_stats()
+    lm_calls = []
+    for _ in range(10):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        samples, _ = env.get_lightmap()
+        lm_calls.append(time.perf_counter() - t0)
+    lm_ms, lm_n = ctx.kernel_stats("lightmap")
+    ctx.set_timing(False)
+    want = pyoracle.lightmap(lit, OP, res["luxels"], res["patch_total"])
+    lm_diff = int(np.count_nonzero(samples.view("<u4").ravel() != want))
+    nlux = env.num_luxels()
+    lm_bytes = 16 * nlux + 16 * nl  # direct light in and sample out per luxel, bounced light per leaf
+    lm_kernel_ms = lm_ms / max(lm_n, 1)
     env.close()
     return {
         "metric": "bounce loop (Jacobi gather to 1e-3 over the built transfer CSR; its build "
@@ -821,6 +845,14 @@ def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
                      "peak_kind": f"{kind} HBM copy", "kernel": "bounce_spmv",
                      "kernel_ms": round(per_iter_ms, 4), "bytes_per_launch": bytes_iter,
                      "reduce_ms": round(red_ms / max(spmv_n, 1), 4)},
+        "lightmap": {"samples": nlux, "kernel_us": round(lm_kernel_ms * 1e3, 2),
+                     "bytes_per_launch": lm_bytes,
+                     "achieved_gbs": round(lm_bytes / (lm_kernel_ms * 1e-3) / 1e9, 1),
+                     "frac_of_hbm": round(lm_bytes / (lm_kernel_ms * 1e-3) / 1e9 / peak, 4),
+                     "call_ms_with_copy": round(1e3 * statistics.median(lm_calls), 3),
+                     "l2": "flushed before each call",
+                     "parity": {"oracle": "orc_lightmap over the device's bake",
+                                "samples_differing": lm_diff, "exact": lm_diff == 0}},
         "clocks": clk,
     }
 
