@@ -729,8 +729,10 @@ def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
     nnz = env.make_transfers(dirs)
     t_xfer = time.perf_counter() - t0
     _, _, ovf = env.transfer_info()
-    rows_ms = ctx.kernel_stats("transfer_rows")[0] + ctx.kernel_stats("transfer_rows_sorted")[0]
+    rows_main_ms = ctx.kernel_stats("transfer_rows")[0]
+    rows_ms = rows_main_ms + ctx.kernel_stats("transfer_rows_sorted")[0]
     xkey = Context.tune_key("transfer_rows", env.num_triangles(), nl * args.k)
+    xv = ctx.autotune_choice(xkey)[0]
     gather_ms = ctx.kernel_stats("transfer_gather")[0]
     ctx.set_timing(False)
     direct = env.gather_patch_direct(nl)
@@ -829,7 +831,15 @@ def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
                       "rays_per_s_M": round(nl * args.k / (rows_ms * 1e-3) / 1e6, 1),
                       "autotune": dict(zip(("bucket", "variant", "variant_ms"),
                                            (xkey,) + ctx.autotune_choice(xkey))),
-                      "patch_build_s": round(t_patch, 3)},
+                      "patch_build_s": round(t_patch, 3),
+                      # the row kernel's closest-hit walks (every row's k rays)
+                      # against the SMs' issue rate
+                      "roofline": dict(issue_roofline(
+                          _profile_value("ncu_transfer_rows.txt",
+                                         f"warp_instructions_per_unit_k{args.k}_v{xv}"),
+                          nl * args.k, rows_main_ms, (clk or {}).get("sm_mhz"), sms,
+                          "profiles/ncu_transfer_rows.txt") or {}, bound="issue",
+                          kernel="transfer_rows", kernel_ms=round(rows_main_ms, 3))},
         "parity": {"transfer_rows_checked": int(len(rows)), "transfer_rows_differing": int(mism),
                    "leaf_direct": dstat,
                    "bounce": {"oracle": "float64 Jacobi over the device's CSR, oracle direct light",
