@@ -583,13 +583,13 @@ def sub_anyhit(args, lib_ctx, stream, dev, flush, l2, sms):
     tv, tms = lib_ctx.autotune_choice(Context.tune_key("trace_mask", env.num_triangles(), n))
     hv, hms = lib_ctx.autotune_choice(Context.tune_key("trace_mask_hit", env.num_triangles(), n))
     # the device's walk, counted by the oracle on the device's tree
-    skip_empty = tv in (12, 13, 14, 15, 16, 17, 18)
+    skip_empty = tv in (12, 13, 14, 15, 16, 17, 18, 19)
     s.set_tree(*env.walk_tree()[:3])
     s.set_skip_empty(skip_empty)
     _, st = s.occlusion_mask(sc.starts, sc.stops, threads=threads, stats=True)
     nodes, tris = st[:, 0].mean(), st[:, 1].mean()
     bytes_per_unit = 24 + 1 / 8 + 8 * nodes + 48 * tris
-    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15, 16, 17, 18) else (
+    prof = "ncu_trace_unit_skip.txt" if tv in (13, 14, 15, 16, 17, 18, 19) else (
         "ncu_trace_unit_stream.txt" if tv in (6, 7, 9, 10, 11) else "ncu_trace_mask.txt")
     peak, kind = _peaks()
     avg_ms = kms / max(kn, 1)

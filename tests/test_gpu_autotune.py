@@ -47,7 +47,7 @@ def test_trace_mask_variants_identical(gpu_ctx, anyhit_scene, tmp_path):
     for closest in (False, True):
         key = Context.tune_key("trace_mask_hit" if closest else "trace_mask", env.num_triangles(), n)
         outs = []
-        for v in range(19):
+        for v in range(20):
             _force(gpu_ctx, tmp_path, key, v)
             outs.append(env.occlusion_mask(a, b, closest=closest))
         for o in outs[1:]:

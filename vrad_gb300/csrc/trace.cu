@@ -143,9 +143,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
     int32_t best = -1;
     float best_t = kInf;
     uint4 stk[kStackMax];
+    unsigned out_of_work = 0u;  // kOptOneVote: the lanes with `exhausted` set (warp-uniform)
     for (;;) {
-        const unsigned idle = __ballot_sync(full, !active && !exhausted);
         const unsigned busy = __ballot_sync(full, active);
+        const unsigned idle = (OPT & kOptOneVote) ? ~busy & ~out_of_work
+                                                  : __ballot_sync(full, !active && !exhausted);
         if (idle == 0 && busy == 0) break;
         if (idle != 0 && (__popc(idle) >= THRESH || busy == 0)) {
             const int leader = __ffs(idle) - 1;
@@ -193,6 +195,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_trace_unit(DevScene s, const
                     }
                 }
             }
+            if (OPT & kOptOneVote) out_of_work = __ballot_sync(full, exhausted);
         }
         bool done = false;
         if (active && lpos == lend && (nd.x & 3u) == 3u) {
@@ -348,7 +351,7 @@ using MaskKernel = void (*)(DevScene, const float *, const float *, int64_t, int
 // lanes, with or without the vote, at the default or a 40-register cap,
 // leaf records kept out of L1 or not, top of the tree in shared memory or
 // not, next plane loaded ahead, children without triangles skipped or not,
-// the walk constants in shared memory or not).
+// the walk constants in shared memory or not, one ballot per round or two).
 const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1>,          k_trace_unit<false, 4, false, 1>,
     k_trace_unit<false, 4, true, 1>, k_trace_unit<false, 8, true, 1>,
@@ -360,7 +363,7 @@ const MaskKernel kMaskOcc[] = {
     k_trace_mask<false, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptSkip>,
     k_trace_unit<false, 8, true, 1, kOptSkip>, k_trace_unit<false, 4, false, 1, kOptStream | kOptSkip>,
     k_trace_unit<false, 4, false, 1, kOptSkip | kOptShRay>, k_trace_unit<false, 8, true, 1, kOptSkip | kOptShRay>,
-    k_trace_unit<false, 8, true, 12, kOptSkip | kOptShRay>,
+    k_trace_unit<false, 8, true, 12, kOptSkip | kOptShRay>, k_trace_unit<false, 8, true, 1, kOptSkip | kOptOneVote>,
 };
 const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1>,          k_trace_unit<true, 4, false, 1>,
@@ -373,9 +376,9 @@ const MaskKernel kMaskHit[] = {
     k_trace_mask<true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptSkip>,
     k_trace_unit<true, 8, true, 1, kOptSkip>, k_trace_unit<true, 4, false, 1, kOptStream | kOptSkip>,
     k_trace_unit<true, 4, false, 1, kOptSkip | kOptShRay>, k_trace_unit<true, 8, true, 1, kOptSkip | kOptShRay>,
-    k_trace_unit<true, 8, true, 12, kOptSkip | kOptShRay>,
+    k_trace_unit<true, 8, true, 12, kOptSkip | kOptShRay>, k_trace_unit<true, 8, true, 1, kOptSkip | kOptOneVote>,
 };
-constexpr int kMaskVariants = 19;
+constexpr int kMaskVariants = 20;
 static_assert(kThreads <= kShRayLanes, "kOptShRay keeps one slot per thread of a block");
 
 }  // namespace

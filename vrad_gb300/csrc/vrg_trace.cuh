@@ -43,6 +43,10 @@ constexpr int kOptSkip = 16;   // children flagged as leaves without triangles a
 // blocks of at most kShRayLanes threads.
 constexpr int kOptShRay = 32;
 constexpr int kShRayLanes = 128;
+// kOptOneVote (unit-round walks): the idle lanes follow from the busy ballot
+// and a warp-wide mask of the lanes out of work, one ballot per round
+// instead of two.
+constexpr int kOptOneVote = 64;
 
 // Shared-memory copy of the scene's top table, for kernels walking with
 // kOptTop (allocated only in kernels that use it).
