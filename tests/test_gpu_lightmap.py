@@ -1,6 +1,7 @@
 """Lightmap samples on the device (vrg_env_get_lightmap): bit-identical to the
 oracle fed the same bake (luxel direct light and leaf bounced light), on a
-small scene and on the 4,096-face bake; face offsets; call-order errors."""
+small scene, on the 4,096-face bake and on faces too large for the kernel's
+shared copy of a face's patch tree; face offsets; call-order errors."""
 import numpy as np
 import pytest
 
@@ -42,6 +43,22 @@ def test_lightmap_matches_oracle(gpu_ctx, oracle, lit_scene, which):
     samples, offsets = env.get_lightmap()
     assert samples.shape == (lit.n_luxels, 4)
     assert np.array_equal(offsets, 4 * lit.luxel_offset())
+    want = oracle.lightmap(lit, P, res["luxels"], res["patch_total"])
+    assert np.array_equal(samples.view("<u4").ravel(), want)
+
+
+def test_lightmap_large_faces_match_oracle(gpu_ctx, oracle):
+    # faces of up to 2,400 units at 32-unit luxels split into more than 128
+    # leaf patches (over 256 tree nodes), more than the kernel's shared copy
+    # holds: those faces are walked in global memory, beside faces that fit
+    from vrad_gb300 import scenes
+
+    lit = scenes.lit_scene(5, n_faces=18, spacing=32.0, n_point=6, n_spot=2, edge=(300.0, 2400.0))
+    env, P = _baked(gpu_ctx, lit, k=64, max_bounces=4)
+    leaves = np.bincount(np.asarray(P["face"])[np.asarray(P["leaf_index"]) >= 0], minlength=lit.n_faces)
+    assert leaves.max() > 128 and leaves.min() <= 128  # both paths run
+    res = env.get_bake(P["n_leaves"])
+    samples, _ = env.get_lightmap()
     want = oracle.lightmap(lit, P, res["luxels"], res["patch_total"])
     assert np.array_equal(samples.view("<u4").ravel(), want)
 
