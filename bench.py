@@ -792,6 +792,7 @@ def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
     bytes_iter = 8 * nnz + 72 * nl  # col+weight per entry; row_ptr, refl, total RMW, emit out per row
     achieved = bytes_iter / (per_iter_ms * 1e-3) / 1e9
     traffic_k = _profile_value("ncu_bounce_spmv.txt", "dram_bytes_per_entry")
+    l2_k = _profile_value("ncu_bounce_spmv.txt", "l2_bytes_per_entry")
     # the lightmap samples of a whole bake of this scene (direct + bounce):
     # the kernel timed per launch with L2 flushed before each call, every
     # sample compared with the oracle's encoding of the same bake
@@ -854,7 +855,16 @@ def sub_radiosity(args, lib_ctx, stream, dev, flush, l2, sms):
                                        "scaled to this nnz)",
                      "peak_kind": f"{kind} HBM copy", "kernel": "bounce_spmv",
                      "kernel_ms": round(per_iter_ms, 4), "bytes_per_launch": bytes_iter,
-                     "reduce_ms": round(red_ms / max(spmv_n, 1), 4)},
+                     "reduce_ms": round(red_ms / max(spmv_n, 1), 4),
+                     # what holds it: the L2-to-SM traffic of the gathers and
+                     # the stream (ncu sectors per entry) against the probe
+                     "l2": ({"achieved": round(l2_k * nnz / (per_iter_ms * 1e-3) / 1e9, 1),
+                             "peak": round(l2, 1), "unit": "GB/s",
+                             "frac": round(l2_k * nnz / (per_iter_ms * 1e-3) / 1e9 / l2, 4),
+                             "bytes_per_entry": l2_k,
+                             "source": "profiles/ncu_bounce_spmv.txt (L2 sectors read per CSR entry); "
+                                       "peak: L2-resident read kernel (probe.cu), timed in this run"}
+                            if l2_k and l2 else None)},
         "lightmap": {"samples": nlux, "kernel_us": round(lm_kernel_ms * 1e3, 2),
                      "bytes_per_launch": lm_bytes,
                      "achieved_gbs": round(lm_bytes / (lm_kernel_ms * 1e-3) / 1e9, 1),
