@@ -99,6 +99,35 @@ def test_gather_points_with_fades_and_exponent(gpu_ctx, oracle, lit_scene):
     assert _rel_err(got, ref).max() <= RTOL
 
 
+def test_wall_cells_holding_more_triangles_than_they_list(gpu_ctx, oracle):
+    # room faces cut into 80 x 80 tiles under a 32 x 32 grid: a cell overlaps
+    # up to 9 tiles (18 triangles) and lists the 8 largest, so many lines
+    # miss the listed ones and are walked; the luxels are the oracle's all
+    # the same, with the cells on or off
+    from vrad_gb300 import scenes
+    from vrad_gb300.environment import Environment
+
+    lit = scenes.lit_scene(8, n_faces=64, n_point=10, n_spot=3, wall_tiles=80)
+    outs = []
+    for cells in (True, False):
+        env = Environment(gpu_ctx)
+        env.set_wall_slots(cells)
+        env.add_triangles(lit.xyz, lit.ids)
+        env.SetupAccelerationStructure()
+        counts = env.wall_slots()[1]
+        assert (counts == 4).sum() == (5 if cells else 0)  # walls and floor, the sky face has none
+        env.set_faces(lit)
+        env.set_lights(lit.lights)
+        outs.append(env.gather_direct_light(supersamples=4, seed=2))
+    assert outs[0][1] == outs[1][1] and np.array_equal(outs[0][0].view(np.uint32),
+                                                       outs[1][0].view(np.uint32))
+    ref, rays = oracle.gather_luxels(oracle.Scene(lit.xyz, lit.ids),
+                                     oracle.make_lights(lit.lights), len(lit.lights), lit, 0,
+                                     lit.n_faces, ss=4, seed=2, threads=16)
+    assert rays == outs[0][1]
+    assert _rel_err(outs[0][0], ref).max() <= RTOL
+
+
 def test_tiled_room_with_and_without_wall_slots(gpu_ctx, oracle):
     # walls split into tiles (as brush sides make them): the gather with the
     # wall slots, without them, and the oracle give the same luxels
