@@ -1,6 +1,7 @@
 """Edge cases through the C ABI on the GPU: empty batches, ragged sizes
 around the 32-line mask words and warp claims, lines starting on a
-triangle's plane, and a relight that changes nothing."""
+triangle's plane (also through every tuned walk variant, with lines along
+the axes), and a relight that changes nothing."""
 import numpy as np
 import pytest
 
@@ -52,6 +53,43 @@ def test_lines_from_triangle_planes(env_and_oracle, anyhit_scene):
     for a, b in ((on, far), (far, on)):
         mask = env.occlusion_mask(a, b)
         assert np.array_equal(mask, osc.occlusion_mask(a, b, threads=16))
+
+
+def test_every_walk_variant_on_plane_and_axis_lines(gpu_ctx, oracle, anyhit_scene, tmp_path):
+    # each tuned form of the shadow-line walk, forced in turn, on lines that
+    # start or end on a triangle's plane and on lines along the axes (zero
+    # direction components, walked through the reciprocal guard): the mask,
+    # hit indices and t equal the oracle's
+    from vrad_gb300.environment import Context, Environment
+
+    xyz = anyhit_scene.xyz.reshape(-1, 3, 3)
+    rng = np.random.default_rng(9)
+    on = xyz[rng.choice(len(xyz), size=1500, replace=False)].mean(axis=1).astype(np.float32)
+    far = rng.uniform(1, 4095, (1500, 3)).astype(np.float32)
+    o = rng.uniform(1, 4095, (1500, 3)).astype(np.float32)
+    ax = o.copy()
+    for i in range(1500):
+        ax[i, i % 3] = np.float32(4095.0 - o[i, i % 3])  # the other two coordinates kept
+    a = np.concatenate([on, far, o])
+    b = np.concatenate([far, on, ax])
+    env = Environment(gpu_ctx)
+    env.add_triangles(anyhit_scene.xyz, anyhit_scene.ids)
+    env.SetupAccelerationStructure()
+    osc = oracle.Scene(anyhit_scene.xyz, anyhit_scene.ids)
+    rmask = osc.occlusion_mask(a, b, threads=16)
+    _, rhit, rt = osc.occlusion_mask(a, b, threads=16, closest=True)
+    for closest in (False, True):
+        key = Context.tune_key("trace_mask_hit" if closest else "trace_mask", env.num_triangles(), len(a))
+        for v in range(20):
+            p = tmp_path / f"tune_{closest}_{v}.txt"
+            p.write_text(f"{key} {v}\n")
+            gpu_ctx.autotune_load(str(p))
+            if closest:
+                m, h, t = env.occlusion_mask(a, b, closest=True)
+                assert np.array_equal(h, rhit) and bits_equal(t, rt), v
+            else:
+                m = env.occlusion_mask(a, b)
+            assert np.array_equal(m, rmask), (closest, v)
 
 
 def test_relight_without_change_keeps_the_bake(gpu_ctx):
