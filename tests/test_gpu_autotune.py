@@ -25,11 +25,13 @@ def test_tune_file_round_trip_host(host_ctx, tmp_path):
     out = tmp_path / "saved.txt"
     host_ctx.autotune_save(str(out))
     assert f"{key} 2" in out.read_text().splitlines()
-    # out-of-range variants in a file are ignored
+    # out-of-range variants in a file are ignored (a site has at most 32)
     bad = tmp_path / "bad.txt"
-    bad.write_text("trace_mask/t1/n1 99\n")
+    bad.write_text("trace_mask/t1/n1 99\ntrace_mask/t2/n2 32\ntrace_mask/t3/n3 -1\n")
     host_ctx.autotune_load(str(bad))
-    assert host_ctx.autotune_choice("trace_mask/t1/n1")[0] == -1
+    for k in ("trace_mask/t1/n1", "trace_mask/t2/n2", "trace_mask/t3/n3"):
+        assert host_ctx.autotune_choice(k)[0] == -1
+    _force(host_ctx, tmp_path, "trace_mask/t4/n4", 31)
 
 
 @pytest.mark.gpu
